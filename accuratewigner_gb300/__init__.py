@@ -1,0 +1,12 @@
+"""GB300-native split-operator propagators with the interface of dibondar/AccurateWigner.
+
+    from accuratewigner_gb300 import WignerMoyalCUDA1D, WignerBlochCUDA1D
+    from accuratewigner_gb300 import RhoVNeumannCUDA1D, RhoBlochCUDA1D, SchrodingerWignerCUDA1D
+
+The classes keep the reference's constructor keywords, attributes and methods;
+the work runs in ``libawigner.so`` (C ABI in ``include/awigner.h``).
+"""
+from .wigner_moyal_cuda_1d import WignerMoyalCUDA1D
+from .wigner_bloch_cuda_1d import WignerBlochCUDA1D
+
+__all__ = ["WignerMoyalCUDA1D", "WignerBlochCUDA1D"]

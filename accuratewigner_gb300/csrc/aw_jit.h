@@ -1,0 +1,338 @@
+// Source of the user-expression module compiled at run time with NVRTC.
+//
+// The reference builds its kernels by str.format()-ing the user's strings
+// (V, K, abs_boundary_*, observables, initial conditions) into CUDA-C
+// templates and compiling them with PyCUDA's SourceModule
+// (wigner_moyal_cuda_1d.py:241-247, :335-342, :400-406).  Here only the small
+// kernels that evaluate those strings are generated: 1-D phase tables, 2-D
+// absorbing masks, initial conditions, observable sums.  The FFT passes that
+// consume the tables are compiled ahead of time (aw_pass.cuh).
+//
+// The user's strings see the same names as in the reference: the #define
+// constants, `t`, the coordinates of the kernel they were written for, the
+// indices i and j, cuda_complex and M_PI.  Every identifier the generated code
+// adds carries an aw_ prefix so that a user #define cannot capture it.
+#pragma once
+#include <string>
+#include <vector>
+
+namespace awjit {
+
+inline const char* prelude() {
+  return R"AWSRC(
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+typedef unsigned long long aw_size_t;
+struct cuda_complex {
+  double _aw_re, _aw_im;
+  __device__ cuda_complex() : _aw_re(0.0), _aw_im(0.0) {}
+  __device__ cuda_complex(double r, double i = 0.0) : _aw_re(r), _aw_im(i) {}
+  __device__ double real() const { return _aw_re; }
+  __device__ double imag() const { return _aw_im; }
+  __device__ cuda_complex& operator+=(const cuda_complex& o) { _aw_re += o._aw_re; _aw_im += o._aw_im; return *this; }
+  __device__ cuda_complex& operator-=(const cuda_complex& o) { _aw_re -= o._aw_re; _aw_im -= o._aw_im; return *this; }
+  __device__ cuda_complex& operator*=(const cuda_complex& o) {
+    double r = _aw_re * o._aw_re - _aw_im * o._aw_im;
+    _aw_im = _aw_re * o._aw_im + _aw_im * o._aw_re; _aw_re = r; return *this; }
+  __device__ cuda_complex& operator/=(const cuda_complex& o) {
+    double d = o._aw_re * o._aw_re + o._aw_im * o._aw_im;
+    double r = (_aw_re * o._aw_re + _aw_im * o._aw_im) / d;
+    _aw_im = (_aw_im * o._aw_re - _aw_re * o._aw_im) / d; _aw_re = r; return *this; }
+};
+__device__ inline cuda_complex operator+(cuda_complex a, const cuda_complex& b) { return a += b; }
+__device__ inline cuda_complex operator-(cuda_complex a, const cuda_complex& b) { return a -= b; }
+__device__ inline cuda_complex operator*(cuda_complex a, const cuda_complex& b) { return a *= b; }
+__device__ inline cuda_complex operator/(cuda_complex a, const cuda_complex& b) { return a /= b; }
+__device__ inline cuda_complex operator-(const cuda_complex& a) { return cuda_complex(-a._aw_re, -a._aw_im); }
+__device__ inline cuda_complex operator+(const cuda_complex& a) { return a; }
+__device__ inline double real(const cuda_complex& a) { return a._aw_re; }
+__device__ inline double imag(const cuda_complex& a) { return a._aw_im; }
+__device__ inline cuda_complex conj(const cuda_complex& a) { return cuda_complex(a._aw_re, -a._aw_im); }
+__device__ inline double abs(const cuda_complex& a) { return hypot(a._aw_re, a._aw_im); }
+__device__ inline double arg(const cuda_complex& a) { return atan2(a._aw_im, a._aw_re); }
+__device__ inline double norm(const cuda_complex& a) { return a._aw_re * a._aw_re + a._aw_im * a._aw_im; }
+__device__ inline cuda_complex exp(const cuda_complex& a) {
+  double e = exp(a._aw_re), s, c; sincos(a._aw_im, &s, &c); return cuda_complex(e * c, e * s); }
+__device__ inline cuda_complex log(const cuda_complex& a) { return cuda_complex(log(abs(a)), arg(a)); }
+__device__ inline cuda_complex pow(const cuda_complex& a, double p) {
+  if (a._aw_re == 0.0 && a._aw_im == 0.0) return cuda_complex(0.0, 0.0);
+  return exp(cuda_complex(p, 0.0) * log(a)); }
+__device__ inline cuda_complex pow(const cuda_complex& a, int p) { return pow(a, (double)p); }
+__device__ inline cuda_complex pow(const cuda_complex& a, const cuda_complex& p) {
+  if (a._aw_re == 0.0 && a._aw_im == 0.0) return cuda_complex(0.0, 0.0);
+  return exp(p * log(a)); }
+__device__ inline cuda_complex pow(double a, const cuda_complex& p) { return exp(p * cuda_complex(log(a), 0.0)); }
+__device__ inline cuda_complex sqrt(const cuda_complex& a) { return pow(a, 0.5); }
+template <typename T> __device__ inline void aw_store(void* aw_p, long long aw_k, int aw_f32, T aw_v);
+template <> __device__ inline void aw_store<double>(void* aw_p, long long aw_k, int aw_f32, double aw_v) {
+  if (aw_f32) ((float2*)aw_p)[aw_k] = make_float2((float)aw_v, 0.f);
+  else ((double2*)aw_p)[aw_k] = make_double2(aw_v, 0.0); }
+template <> __device__ inline void aw_store<cuda_complex>(void* aw_p, long long aw_k, int aw_f32, cuda_complex aw_v) {
+  if (aw_f32) ((float2*)aw_p)[aw_k] = make_float2((float)aw_v._aw_re, (float)aw_v._aw_im);
+  else ((double2*)aw_p)[aw_k] = make_double2(aw_v._aw_re, aw_v._aw_im); }
+__device__ inline double2 aw_load(const void* aw_p, long long aw_k, int aw_f32) {
+  if (aw_f32) { float2 aw_v = ((const float2*)aw_p)[aw_k]; return make_double2(aw_v.x, aw_v.y); }
+  return ((const double2*)aw_p)[aw_k]; }
+__device__ inline double aw_block_sum(double aw_v, double* aw_red) {
+  const int aw_t = threadIdx.x;
+  aw_red[aw_t] = aw_v;
+  __syncthreads();
+  for (int aw_w = blockDim.x / 2; aw_w > 0; aw_w >>= 1) {
+    if (aw_t < aw_w) aw_red[aw_t] += aw_red[aw_t + aw_w];
+    __syncthreads();
+  }
+  double aw_r = aw_red[0];
+  __syncthreads();
+  return aw_r;
+}
+)AWSRC";
+}
+
+// coordinate names of each propagator kind, as the reference's kernels declare them
+struct KindNames {
+  bool rotated;     // WM/WB: (XX, XX_prime) and (PP, PP_prime) grids, 2-D masks
+  bool vn;          // VN/RB: abs_boundary_x(X), abs_boundary_p(P) functions
+  bool sw;          // SW: 1-D wave function
+};
+
+inline std::string module_source(const KindNames& kn, const std::string& consts, const std::string& V,
+                                 const std::string& K, const std::string& absx, const std::string& absp,
+                                 const std::vector<std::string>& obs_x, const std::vector<std::string>& obs_p) {
+  std::string s = prelude();
+  s += "\n// ---- user constants and functions\n";
+  s += consts;
+  s += "\n// ---- energies (wigner_moyal_cuda_1d.py:723-733)\n";
+  s += "__device__ double K(double P, double t) { return (" + K + "); }\n";
+  s += "__device__ double V(double X, double t) { return (" + V + "); }\n";
+  if (kn.rotated) {
+    s += "__device__ double aw_absx2d(aw_size_t i, aw_size_t j, double XX, double XX_prime, double PP, double PP_prime, double t) { return (" + absx + "); }\n";
+    s += "__device__ double aw_absp2d(aw_size_t i, aw_size_t j, double XX, double XX_prime, double PP, double PP_prime, double t) { return (" + absp + "); }\n";
+    s += "__device__ double aw_mask1(int aw_fn, aw_size_t j, double aw_x, double t) { return 1.0; }\n";
+  } else if (kn.vn) {
+    s += "__device__ double abs_boundary_x(double X) { return (" + absx + "); }\n";
+    s += "__device__ double abs_boundary_p(double P) { return (" + absp + "); }\n";
+    s += "__device__ double aw_mask1(int aw_fn, aw_size_t j, double aw_x, double t) { return aw_fn == 0 ? abs_boundary_x(aw_x) : abs_boundary_p(aw_x); }\n";
+  } else {
+    s += "__device__ double aw_absx1(aw_size_t j, double X, double t) { return (" + absx + "); }\n";
+    s += "__device__ double aw_absp1(aw_size_t j, double P, double t) { return (" + absp + "); }\n";
+    s += "__device__ double aw_mask1(int aw_fn, aw_size_t j, double aw_x, double t) { return aw_fn == 0 ? aw_absx1(j, aw_x, t) : aw_absp1(j, aw_x, t); }\n";
+  }
+  s += "__device__ double aw_obs_x(int aw_k, double X, double t) {\n  switch (aw_k) {\n";
+  for (size_t k = 0; k < obs_x.size(); ++k) s += "    case " + std::to_string(k) + ": return (" + obs_x[k] + ");\n";
+  s += "  }\n  return 0.0;\n}\n";
+  s += "__device__ double aw_obs_p(int aw_k, double P, double t) {\n  switch (aw_k) {\n";
+  for (size_t k = 0; k < obs_p.size(); ++k) s += "    case " + std::to_string(k) + ": return (" + obs_p[k] + ");\n";
+  s += "  }\n  return 0.0;\n}\n";
+  s += R"AWSRC(
+// 1-D tables of phase factors.  Column entries (aw_ncol of them) sit on the
+// grid x_j = aw_dcol (((j + aw_roll) mod aw_ncol) - aw_ncol/2), row entries on
+// x_i = aw_drow (i - aw_nrow/2).  aw_mode 0: exp(i (ca F(x,ta) + cb F(x,tb)));
+// aw_mode 1: exp(ca (F(x,ta) - shift)) (real).  F = V (aw_fn 0) or K (aw_fn 1).
+// aw_maskpow > 0 multiplies by the one-dimensional absorbing boundary.
+extern "C" __global__ void aw_tab(void* aw_col, void* aw_row, int aw_f32, int aw_fn, int aw_mode,
+                                  int aw_ncol, double aw_dcol, int aw_roll, int aw_nrow, double aw_drow,
+                                  double aw_ta, double aw_tb, double aw_ca, double aw_cb, double aw_shift,
+                                  int aw_maskpow, double aw_tmask) {
+  const int aw_k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (aw_k >= aw_ncol + aw_nrow) return;
+  const bool aw_c = aw_k < aw_ncol;
+  const int aw_n = aw_c ? aw_ncol : aw_nrow;
+  const int aw_idx = aw_c ? aw_k : aw_k - aw_ncol;
+  const aw_size_t aw_m = aw_c ? (aw_size_t)((aw_idx + aw_roll) % aw_n) : (aw_size_t)aw_idx;
+  const double aw_x = (aw_c ? aw_dcol : aw_drow) * (aw_m - 0.5 * aw_n);
+  double aw_re, aw_im;
+  if (aw_mode == 0) {
+    double aw_ph = aw_ca * (aw_fn == 0 ? V(aw_x, aw_ta) : K(aw_x, aw_ta));
+    if (aw_cb != 0.0) aw_ph += aw_cb * (aw_fn == 0 ? V(aw_x, aw_tb) : K(aw_x, aw_tb));
+    sincos(aw_ph, &aw_im, &aw_re);
+  } else {
+    aw_re = exp(aw_ca * ((aw_fn == 0 ? V(aw_x, aw_ta) : K(aw_x, aw_ta)) - aw_shift));
+    aw_im = 0.0;
+  }
+  if (aw_maskpow > 0) {
+    double aw_q = aw_mask1(aw_fn, aw_m, aw_x, aw_tmask);
+    double aw_f = aw_maskpow == 2 ? aw_q * aw_q : aw_q;
+    aw_re *= aw_f;
+    aw_im *= aw_f;
+  }
+  void* aw_dst = aw_c ? aw_col : aw_row;
+  if (aw_f32) ((float2*)aw_dst)[aw_idx] = make_float2((float)aw_re, (float)aw_im);
+  else ((double2*)aw_dst)[aw_idx] = make_double2(aw_re, aw_im);
+}
+
+// Plain values of V or K on a 1-D grid (Bloch minima, rho_bloch/wigner_bloch fill kernels).
+extern "C" __global__ void aw_values(double* aw_out, int aw_fn, int aw_n, double aw_d, double aw_t) {
+  const int aw_k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (aw_k >= aw_n) return;
+  const double aw_x = aw_d * ((aw_size_t)aw_k - 0.5 * aw_n);
+  aw_out[aw_k] = aw_fn == 0 ? V(aw_x, aw_t) : K(aw_x, aw_t);
+}
+
+// Per-step observables from the marginals of the (unnormalised) Wigner
+// function: colsum[j] = Sum_i Re W[i][j], rowpart[p][i] = partial row sums.
+// Writes slots (sums of X-only and P-only averages, normalised as
+// wigner_moyal_cuda_1d.py:608-622 normalises W), the purity 2 pi Sum W^2 dXdP
+// of the normalised W, the norm, and 1 / norm for the next pass.
+extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw_rowpart, int aw_nparts,
+                                       const double* aw_sqpart, double* aw_rowsum, double* aw_hist,
+                                       double* aw_inv_norm, int* aw_stop, int aw_stop_on_purity, double t,
+                                       int aw_ncol, int aw_nrow, double aw_dX, double aw_dP, double aw_dXdP,
+                                       const int* aw_tslot, const int* aw_tkind, const int* aw_tidx,
+                                       const double* aw_tcoef, int aw_nterms, int aw_nslots) {
+  __shared__ double aw_red[256];
+  __shared__ double aw_tv[64];
+  if (aw_stop && *aw_stop) return;
+  const int aw_t = threadIdx.x;
+  const int aw_nt = blockDim.x;
+  for (int aw_i = aw_t; aw_i < aw_nrow; aw_i += aw_nt) {
+    double aw_s = 0.0;
+    for (int aw_p = 0; aw_p < aw_nparts; ++aw_p) aw_s += aw_rowpart[(long long)aw_p * aw_nrow + aw_i];
+    aw_rowsum[aw_i] = aw_s;
+  }
+  __syncthreads();
+  double aw_s = 0.0;
+  for (int aw_j = aw_t; aw_j < aw_ncol; aw_j += aw_nt) aw_s += aw_colsum[aw_j];
+  const double aw_norm_raw = aw_block_sum(aw_s, aw_red);
+  aw_s = 0.0;
+  for (int aw_p = aw_t; aw_p < aw_nparts; aw_p += aw_nt) aw_s += aw_sqpart[aw_p];
+  const double aw_sq = aw_block_sum(aw_s, aw_red);
+  for (int aw_k = 0; aw_k < aw_nterms && aw_k < 64; ++aw_k) {
+    aw_s = 0.0;
+    const int aw_idx = aw_tidx[aw_k];
+    if (aw_tkind[aw_k] == 0) {
+      for (int aw_j = aw_t; aw_j < aw_ncol; aw_j += aw_nt) {
+        const double X = aw_dX * ((aw_size_t)aw_j - 0.5 * aw_ncol);
+        aw_s += aw_colsum[aw_j] * aw_obs_x(aw_idx, X, t);
+      }
+    } else {
+      for (int aw_i = aw_t; aw_i < aw_nrow; aw_i += aw_nt) {
+        const double P = aw_dP * ((aw_size_t)aw_i - 0.5 * aw_nrow);
+        aw_s += aw_rowsum[aw_i] * aw_obs_p(aw_idx, P, t);
+      }
+    }
+    const double aw_v = aw_block_sum(aw_s, aw_red);
+    if (aw_t == 0) aw_tv[aw_k] = aw_v;
+  }
+  if (aw_t == 0) {
+    const double aw_norm = aw_norm_raw * aw_dXdP;
+    for (int aw_q = 0; aw_q < aw_nslots; ++aw_q) aw_hist[aw_q] = 0.0;
+    for (int aw_k = 0; aw_k < aw_nterms && aw_k < 64; ++aw_k)
+      aw_hist[aw_tslot[aw_k]] += aw_tcoef[aw_k] * (aw_tv[aw_k] * aw_dXdP / aw_norm);
+    const double aw_purity = 2.0 * M_PI * aw_sq * aw_dXdP / (aw_norm * aw_norm);
+    aw_hist[aw_nslots] = aw_purity;
+    aw_hist[aw_nslots + 1] = aw_norm;
+    *aw_inv_norm = 1.0 / aw_norm;
+    if (aw_stop && aw_stop_on_purity && !(aw_purity < 1.0)) *aw_stop = 1;
+  }
+}
+)AWSRC";
+  if (kn.rotated) {
+    s += R"AWSRC(
+// 2-D absorbing boundaries of the rotated frame (expV / expK of
+// wigner_moyal_cuda_1d.py:742-778 multiply by these expressions).
+extern "C" __global__ void aw_mask2d(void* aw_out, int aw_f32, int aw_which, double t, int aw_nrow, int aw_ncol,
+                                     double aw_dXX, double aw_dXXp, double aw_dPP, double aw_dPPp) {
+  const aw_size_t i = blockIdx.y;
+  const aw_size_t j = (aw_size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= (aw_size_t)aw_ncol) return;
+  const double XX = aw_dXX * (j - 0.5 * aw_ncol);
+  const double XX_prime = aw_dXXp * (i - 0.5 * aw_nrow);
+  const double PP = aw_dPP * (j - 0.5 * aw_ncol);
+  const double PP_prime = aw_dPPp * (i - 0.5 * aw_nrow);
+  const double aw_v = aw_which == 0 ? aw_absx2d(i, j, XX, XX_prime, PP, PP_prime, t)
+                                    : aw_absp2d(i, j, XX, XX_prime, PP, PP_prime, t);
+  const long long aw_k = (long long)i * aw_ncol + j;
+  if (aw_f32) ((float*)aw_out)[aw_k] = (float)aw_v;
+  else ((double*)aw_out)[aw_k] = aw_v;
+}
+)AWSRC";
+  }
+  return s;
+}
+
+// Initial condition module (one per expression string).
+inline std::string init_source(const KindNames& kn, const std::string& consts, const std::string& expr) {
+  std::string s = prelude();
+  s += consts;
+  s += "\n";
+  if (kn.rotated) {
+    // wigner_moyal_cuda_1d.py:791-801
+    s += "extern \"C\" __global__ void aw_init(void* aw_out, int aw_f32, int aw_nrow, int aw_ncol, double aw_dX, double aw_dP) {\n"
+         "  const aw_size_t i = blockIdx.y;\n"
+         "  const aw_size_t j = (aw_size_t)blockIdx.x * blockDim.x + threadIdx.x;\n"
+         "  if (j >= (aw_size_t)aw_ncol) return;\n"
+         "  const double X = aw_dX * (j - 0.5 * aw_ncol);\n"
+         "  const double P = aw_dP * (i - 0.5 * aw_nrow);\n"
+         "  aw_store(aw_out, (long long)i * aw_ncol + j, aw_f32, (" + expr + "));\n}\n";
+  } else if (kn.vn) {
+    // rho_vneumann_cuda_1d.py:783-793
+    s += "extern \"C\" __global__ void aw_init(void* aw_out, int aw_f32, int aw_nrow, int aw_ncol, double aw_dX, double aw_dP) {\n"
+         "  const aw_size_t i = blockIdx.y;\n"
+         "  const aw_size_t j = (aw_size_t)blockIdx.x * blockDim.x + threadIdx.x;\n"
+         "  if (j >= (aw_size_t)aw_ncol) return;\n"
+         "  const double X = aw_dX * (j - 0.5 * aw_ncol);\n"
+         "  const double X_prime = aw_dX * (i - 0.5 * aw_nrow);\n"
+         "  aw_store(aw_out, (long long)i * aw_ncol + j, aw_f32, (" + expr + "));\n}\n";
+  } else {
+    // schrodinger_wigner_cuda_1d.py:867-874
+    s += "extern \"C\" __global__ void aw_init(void* aw_out, int aw_f32, int aw_nrow, int aw_ncol, double aw_dX, double aw_dP) {\n"
+         "  const aw_size_t j = (aw_size_t)blockIdx.x * blockDim.x + threadIdx.x;\n"
+         "  if (j >= (aw_size_t)aw_ncol) return;\n"
+         "  const double X = aw_dX * (j - 0.5 * aw_ncol);\n"
+         "  aw_store(aw_out, (long long)j, aw_f32, (" + expr + "));\n}\n";
+  }
+  return s;
+}
+
+// Observable module (one per expression string).
+//   rotated: partial sums of Re W f(X, P, t) over the Wigner grid (wm:817-827)
+//   vn:      rho[i][j] *= f(X, P, t), X and P both from column j (vn:811-821)
+//   sw:      partial sums of |psi|^2 f(X, P, t), P fft-shifted (sw:893-901)
+inline std::string observable_source(const KindNames& kn, const std::string& consts, const std::string& expr) {
+  std::string s = prelude();
+  s += consts;
+  s += "\n";
+  if (kn.rotated) {
+    s += "extern \"C\" __global__ void aw_obs(const void* aw_W, int aw_f32, double t, double* aw_part, int aw_nrow, int aw_ncol, double aw_dX, double aw_dP) {\n"
+         "  __shared__ double aw_red[256];\n"
+         "  double aw_s = 0.0;\n"
+         "  const long long aw_n = (long long)aw_nrow * aw_ncol;\n"
+         "  for (long long aw_k = (long long)blockIdx.x * blockDim.x + threadIdx.x; aw_k < aw_n; aw_k += (long long)gridDim.x * blockDim.x) {\n"
+         "    const aw_size_t i = aw_k / aw_ncol;\n"
+         "    const aw_size_t j = aw_k - (long long)i * aw_ncol;\n"
+         "    const double X = aw_dX * (j - 0.5 * aw_ncol);\n"
+         "    const double P = aw_dP * (i - 0.5 * aw_nrow);\n"
+         "    aw_s += aw_load(aw_W, aw_k, aw_f32).x * (" + expr + ");\n"
+         "  }\n"
+         "  aw_s = aw_block_sum(aw_s, aw_red);\n"
+         "  if (threadIdx.x == 0) aw_part[blockIdx.x] = aw_s;\n}\n";
+  } else if (kn.vn) {
+    s += "extern \"C\" __global__ void aw_obs(void* aw_rho, int aw_f32, double t, double* aw_unused, int aw_nrow, int aw_ncol, double aw_dX, double aw_dP) {\n"
+         "  const aw_size_t i = blockIdx.y;\n"
+         "  const aw_size_t j = (aw_size_t)blockIdx.x * blockDim.x + threadIdx.x;\n"
+         "  if (j >= (aw_size_t)aw_ncol) return;\n"
+         "  const double P = aw_dP * (j - 0.5 * aw_ncol);\n"
+         "  const double X = aw_dX * (j - 0.5 * aw_ncol);\n"
+         "  const long long aw_k = (long long)i * aw_ncol + j;\n"
+         "  double2 aw_v = aw_load(aw_rho, aw_k, aw_f32);\n"
+         "  cuda_complex aw_r = cuda_complex(aw_v.x, aw_v.y) * cuda_complex(" + expr + ");\n"
+         "  aw_store(aw_rho, aw_k, aw_f32, aw_r);\n}\n";
+  } else {
+    s += "extern \"C\" __global__ void aw_obs(const void* aw_psi, int aw_f32, double t, double* aw_part, int aw_nrow, int aw_ncol, double aw_dX, double aw_dP) {\n"
+         "  __shared__ double aw_red[256];\n"
+         "  double aw_s = 0.0;\n"
+         "  for (long long aw_k = (long long)blockIdx.x * blockDim.x + threadIdx.x; aw_k < aw_ncol; aw_k += (long long)gridDim.x * blockDim.x) {\n"
+         "    const aw_size_t j = aw_k;\n"
+         "    const double X = aw_dX * (j - 0.5 * aw_ncol);\n"
+         "    const double P = aw_dP * ((j + aw_ncol / 2) % aw_ncol - 0.5 * aw_ncol);\n"
+         "    double2 aw_v = aw_load(aw_psi, aw_k, aw_f32);\n"
+         "    aw_s += (aw_v.x * aw_v.x + aw_v.y * aw_v.y) * (" + expr + ");\n"
+         "  }\n"
+         "  aw_s = aw_block_sum(aw_s, aw_red);\n"
+         "  if (threadIdx.x == 0) aw_part[blockIdx.x] = aw_s;\n}\n";
+  }
+  return s;
+}
+
+}  // namespace awjit

@@ -1,0 +1,76 @@
+// Argument blocks of the fused FFT pass kernels (host and device side).
+//
+// One pass reads a tile of whole lines (rows or columns of the grid) once,
+// runs a short fixed program on it in shared memory and writes it once:
+//
+//   load -> f0 -> [FFT d1] -> f1 -> (branch point) -> f2 -> [FFT d2] -> f3 -> store/reduce
+//                                       |
+//                                       +-> [FFT br_d1] -> fbr -> [FFT br_d2] -> store br_out
+//
+// which covers every cuFFT-plus-elementwise sequence of the reference's steps
+// (wigner_moyal_cuda_1d.py:543-561), Wigner transforms (:422-501) and Bloch
+// steps (wigner_bloch_cuda_1d.py:221-240).
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+// Per-element multiplier.  Every field is optional; the product of the active
+// parts is applied:  scale * (*scale_ptr) * (-1)^(i+j) * col_tab[j]
+//                     * conj(row_tab[i]) * mask[i][j]^mask_pow * shear(line, pos)
+typedef struct AwFactor {
+  const void* col_tab;      // complex, one per grid column j
+  const void* row_tab;      // complex, one per grid row i (used conjugated)
+  const void* mask;         // real, [nrows][ncols]
+  const void* sh_hi;        // shear table, [lines][npos / sh_lo_n] complex
+  const void* sh_lo;        // shear table, [lines][sh_lo_n] complex
+  const double* scale_ptr;  // optional device scalar: complex (re, im), one per instance
+  double scale;
+  int mask_pow;             // 0: no mask
+  int sign;                 // multiply by (-1)^(i+j)
+  int sh_lo_n;              // 0: no shear
+  int sh_roll;              // shear position index is (pos + sh_roll) mod npos
+  int active;
+} AwFactor;
+
+typedef struct AwPassArgs {
+  const void* in;
+  void* out;                // may be 0 for a reduce-only pass
+  int nrows, ncols;
+  const void* tw;           // twiddle table of the transform length
+  AwFactor f0;
+  int d1;                   // 0: none, +1: forward, -1: inverse (unnormalised)
+  AwFactor f1;
+  void* mid_out;            // optional store of the tile at the branch point
+  int mid_sign;             // ... multiplied by (-1)^(i+j)
+  void* br_out;             // optional branch output
+  int br_d1;
+  AwFactor fbr;
+  int br_d2;
+  AwFactor f2;
+  int d2;
+  AwFactor f3;
+  double* red_line;         // column pass: per column, sum of Re
+  double* red_cross;        // column pass: [block][row], sum of Re over the block's columns
+  double* red_sq;           // column pass: [block], sum of Re(v*v)
+  double2* diag_out;        // row pass: element (i, i) at the branch point
+  double* red_abs2;         // row pass: [block], sum of |v|^2 at the branch point
+  const int* stop;          // when non-zero the pass is skipped
+  long long batch_elems;    // batched launches: elements per instance (blockIdx.y)
+  long long batch_tab;      // ... table entries per instance
+} AwPassArgs;
+
+// Host-side launchers, one per precision (aw_pass_f64.cu / aw_pass_f32.cu).
+// Returns 0 on success, or a negative code when the size is unsupported.
+int aw_launch_row_pass_f64(const AwPassArgs* a, int batch, void* stream);
+int aw_launch_col_pass_f64(const AwPassArgs* a, int batch, void* stream);
+int aw_launch_row_pass_f32(const AwPassArgs* a, int batch, void* stream);
+int aw_launch_col_pass_f32(const AwPassArgs* a, int batch, void* stream);
+// number of column blocks (rows of red_cross) the column pass uses for a given N
+int aw_col_pass_blocks(int nrows, int ncols, int f32);
+
+#ifdef __cplusplus
+}
+#endif

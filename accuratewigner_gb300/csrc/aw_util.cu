@@ -1,0 +1,197 @@
+// Element-wise and reduction kernels that need no user expression.
+//
+// Reductions are deterministic: a fixed grid of blocks writes one partial
+// each and the partials are summed in index order, so repeated runs (and a
+// propagation run alone or inside a batch) give bit-identical scalars.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "aw_util.h"
+
+namespace {
+
+__device__ __forceinline__ double2 ld(const void* p, long long k, int f32) {
+  if (f32) {
+    float2 v = ((const float2*)p)[k];
+    return make_double2(v.x, v.y);
+  }
+  return ((const double2*)p)[k];
+}
+__device__ __forceinline__ void st(void* p, long long k, int f32, double2 v) {
+  if (f32)
+    ((float2*)p)[k] = make_float2((float)v.x, (float)v.y);
+  else
+    ((double2*)p)[k] = v;
+}
+
+__global__ void k_scale(void* a, int f32, long long n, double re, double im, const double* ptr) {
+  double sr = re, si = im;
+  if (ptr) {
+    const double pr = ptr[0], pi = ptr[1];
+    sr = re * pr - im * pi;
+    si = re * pi + im * pr;
+  }
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    double2 v = ld(a, k, f32);
+    st(a, k, f32, make_double2(v.x * sr - v.y * si, v.x * si + v.y * sr));
+  }
+}
+
+__global__ void k_fill(void* a, int f32, long long n, double re, double im) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    st(a, k, f32, make_double2(re, im));
+}
+
+__global__ void k_convert(const void* src, int sf32, void* dst, int df32, long long n) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    st(dst, k, df32, ld(src, k, sf32));
+}
+
+// mode 0: sum of a; 1: sum of Re(a*a); 2: sum of |a|^2; 3: trace (n = N, stride N+1)
+__global__ void k_partial(const void* a, int f32, long long n, int mode, long long stride, double2* part) {
+  __shared__ double rr[256], ri[256];
+  double sr = 0.0, si = 0.0;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    double2 v = ld(a, mode == 3 ? k * stride : k, f32);
+    if (mode == 0 || mode == 3) {
+      sr += v.x;
+      si += v.y;
+    } else if (mode == 1) {
+      sr += v.x * v.x - v.y * v.y;
+    } else {
+      sr += v.x * v.x + v.y * v.y;
+    }
+  }
+  const int t = threadIdx.x;
+  rr[t] = sr;
+  ri[t] = si;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (t < w) {
+      rr[t] += rr[t + w];
+      ri[t] += ri[t + w];
+    }
+    __syncthreads();
+  }
+  if (t == 0) part[blockIdx.x] = make_double2(rr[0], ri[0]);
+}
+
+__global__ void k_embed(const void* rho, int f32, int N, void* W, int M, int pad) {
+  const long long n = (long long)M * M;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(k / M), j = (int)(k - (long long)i * M);
+    double2 v = make_double2(0.0, 0.0);
+    if (i >= pad && i < pad + N && j >= pad && j < pad + N) v = ld(rho, (long long)(i - pad) * N + (j - pad), f32);
+    st(W, k, f32, v);
+  }
+}
+
+__global__ void k_psi2rho(const void* psi, int f32, int N, void* rho) {
+  const long long n = (long long)N * N;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(k / N), j = (int)(k - (long long)i * N);
+    const double2 a = ld(psi, j, f32), b = ld(psi, i, f32);
+    // psi[j] * conj(psi[i])   (schrodinger_wigner_cuda_1d.py:680-687)
+    st(rho, k, f32, make_double2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y));
+  }
+}
+
+// von Neumann / rho-Bloch per-step normalisation from the diagonal gathered by
+// the row pass:  inv = 1 / (Re Tr rho * dX)  (rho_vneumann_cuda_1d.py:443) or
+// 1 / (Tr rho * dX) with the complex trace (rho_bloch_cuda_1d.py:244).  The
+// purity Sum |rho|^2 dX^2 (rho_vneumann_cuda_1d.py:565-579) of the normalised
+// state follows from the row pass's |rho|^2 partials.
+__global__ void k_trace_finalize(const double2* diag, int n, const double* abs2part, int nparts, double dX,
+                                 int complex_trace, double* inv_out, double* hist, int* stop, int stop_on_purity) {
+  __shared__ double rr[256], ri[256], ra[256];
+  if (stop && *stop) return;
+  const int t = threadIdx.x;
+  double sr = 0.0, si = 0.0, sa = 0.0;
+  for (int k = t; k < n; k += blockDim.x) {
+    sr += diag[k].x;
+    si += diag[k].y;
+  }
+  if (abs2part)
+    for (int k = t; k < nparts; k += blockDim.x) sa += abs2part[k];
+  rr[t] = sr;
+  ri[t] = si;
+  ra[t] = sa;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (t < w) {
+      rr[t] += rr[t + w];
+      ri[t] += ri[t + w];
+      ra[t] += ra[t + w];
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    const double tr = rr[0] * dX, ti = complex_trace ? ri[0] * dX : 0.0;
+    const double d = tr * tr + ti * ti;
+    const double ir = tr / d, ii = -ti / d;
+    inv_out[0] = ir;
+    inv_out[1] = ii;
+    const double purity = ra[0] * (ir * ir + ii * ii) * dX * dX;
+    if (hist) {
+      hist[0] = purity;
+      hist[1] = tr;
+      hist[2] = ti;
+    }
+    if (stop && stop_on_purity && !(purity < 1.0)) *stop = 1;
+  }
+}
+
+__global__ void k_set2(double* p, double a, double b) {
+  p[0] = a;
+  p[1] = b;
+}
+
+inline int grid_for(long long n) {
+  long long g = (n + 255) / 256;
+  if (g > 4 * 152 * 8) g = 4 * 152 * 8;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+inline int ok() { return cudaGetLastError() == cudaSuccess ? 0 : -1; }
+
+}  // namespace
+
+extern "C" {
+
+int aw_k_scale(void* a, int f32, long long n, double re, double im, const double* ptr, void* s) {
+  k_scale<<<grid_for(n), 256, 0, (cudaStream_t)s>>>(a, f32, n, re, im, ptr);
+  return ok();
+}
+int aw_k_fill(void* a, int f32, long long n, double re, double im, void* s) {
+  k_fill<<<grid_for(n), 256, 0, (cudaStream_t)s>>>(a, f32, n, re, im);
+  return ok();
+}
+int aw_k_convert(const void* src, int sf32, void* dst, int df32, long long n, void* s) {
+  k_convert<<<grid_for(n), 256, 0, (cudaStream_t)s>>>(src, sf32, dst, df32, n);
+  return ok();
+}
+int aw_k_partial(const void* a, int f32, long long n, int mode, long long stride, double2* part, int nblocks, void* s) {
+  k_partial<<<nblocks, 256, 0, (cudaStream_t)s>>>(a, f32, n, mode, stride, part);
+  return ok();
+}
+int aw_k_embed(const void* rho, int f32, int N, void* W, int M, int pad, void* s) {
+  k_embed<<<grid_for((long long)M * M), 256, 0, (cudaStream_t)s>>>(rho, f32, N, W, M, pad);
+  return ok();
+}
+int aw_k_psi2rho(const void* psi, int f32, int N, void* rho, void* s) {
+  k_psi2rho<<<grid_for((long long)N * N), 256, 0, (cudaStream_t)s>>>(psi, f32, N, rho);
+  return ok();
+}
+int aw_k_trace_finalize(const double2* diag, int n, const double* abs2part, int nparts, double dX, int complex_trace,
+                        double* inv_out, double* hist, int* stop, int stop_on_purity, void* s) {
+  k_trace_finalize<<<1, 256, 0, (cudaStream_t)s>>>(diag, n, abs2part, nparts, dX, complex_trace, inv_out, hist, stop,
+                                                   stop_on_purity);
+  return ok();
+}
+int aw_k_set2(double* p, double a, double b, void* s) {
+  k_set2<<<1, 1, 0, (cudaStream_t)s>>>(p, a, b);
+  return ok();
+}
+
+}  // extern "C"

@@ -1,0 +1,194 @@
+/* awigner.h -- C ABI of the GB300 split-operator propagators.
+ *
+ * The reference (dibondar/AccurateWigner) is Python 2 + PyCUDA: each propagator
+ * class pastes CUDA-C expression strings into kernel templates, compiles them
+ * with nvcc at construction and drives cuFFT through ctypes.  This library is
+ * the native layer beneath drop-in Python classes with the same names; every
+ * entry point below names the reference method it replaces.  Citations are
+ * file:line inside the reference project.
+ *
+ * Conventions
+ *   - Every call returns AW_OK (0) or a negative AW_E_* code; the message of the
+ *     last failure on the calling thread is available from aw_last_error().
+ *   - Complex buffers are interleaved (re, im) and C-ordered [row][column],
+ *     rows = P / X' index, columns = X index, as in the reference.
+ *   - A handle owns its device buffers and one CUDA stream; it is not
+ *     thread-safe.  Calls are stream-ordered; calls that return data to the host
+ *     synchronise the stream.
+ */
+#ifndef AWIGNER_H
+#define AWIGNER_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AW_OK 0
+#define AW_E_ARG -1      /* invalid argument (Python maps to AssertionError / ValueError) */
+#define AW_E_CUDA -2     /* CUDA runtime failure */
+#define AW_E_JIT -3      /* NVRTC compile error of a user expression (RuntimeError) */
+#define AW_E_STATE -4    /* call not valid for this propagator kind or state */
+#define AW_E_NOMEM -5    /* device allocation failed */
+
+/* propagator kinds */
+#define AW_WIGNER_MOYAL 0   /* WignerMoyalCUDA1D       wigner_moyal_cuda_1d.py:10 */
+#define AW_WIGNER_BLOCH 1   /* WignerBlochCUDA1D       wigner_bloch_cuda_1d.py:9 */
+#define AW_RHO_VNEUMANN 2   /* RhoVNeumannCUDA1D       rho_vneumann_cuda_1d.py:15 */
+#define AW_RHO_BLOCH 3      /* RhoBlochCUDA1D          rho_bloch_cuda_1d.py:10 */
+#define AW_SCHRODINGER 4    /* SchrodingerWignerCUDA1D schrodinger_wigner_cuda_1d.py:16 */
+
+/* arithmetic of the state */
+#define AW_C128 0           /* complex128 throughout, as the reference (wigner_moyal_cuda_1d.py:629) */
+#define AW_C64 1            /* complex64 butterflies and phases; FP64 tables and reductions */
+
+/* device buffers */
+#define AW_BUF_RHO 0        /* rho (WM/WB: Np x Nx in the rotated frame; VN/RB: N x N) */
+#define AW_BUF_WIGNER 1     /* wignerfunction (WM/WB: Np x Nx; VN/RB: 2N x 2N; SW: N x N) */
+#define AW_BUF_PSI 2        /* wavefunction (SW: 1 x N) */
+#define AW_BUF_SNAPSHOT 3   /* copy of rho / psi used by ground-state rollback */
+
+/* spatial classes of an observable term */
+#define AW_TERM_X 0         /* expression of X (and t) only */
+#define AW_TERM_P 1         /* expression of P (and t) only */
+
+typedef struct aw_state_s* aw_handle;
+
+typedef struct aw_config {
+  int32_t kind;
+  int32_t precision;
+  int32_t x_grid_dim;        /* X_gridDIM */
+  int32_t p_grid_dim;        /* P_gridDIM (WM/WB); ignored otherwise */
+  /* kernel constants, already rounded through "%.15e" as the reference's
+   * #defines round them (wigner_moyal_cuda_1d.py:171-176) */
+  double dX, dP;
+  double dXX, dXX_prime, dPP, dPP_prime;   /* WM/WB rotated grids (wm:122-134); VN: dXX = dX, dPP */
+  double dt;
+  double t_initial;
+  double dXdP;               /* measure of the Wigner grid used by averages and norms */
+  /* source of the user module: the reference's cuda_consts string (all
+   * #defines + consts + functions) and the expression strings */
+  const char* cuda_consts;
+  const char* V;
+  const char* K;
+  const char* abs_boundary_x;
+  const char* abs_boundary_p;
+  int32_t v_time_dependent;  /* V mentions t: phase tables are rebuilt every step */
+  int32_t k_time_dependent;
+  int32_t absx_mode;         /* 0: identically one; 1: fixed in time; 2: depends on t */
+  int32_t absp_mode;
+  /* observables recorded every step (Ehrenfest theorems and energy,
+   * wigner_moyal_cuda_1d.py:584-606) as sums of X-only and P-only terms */
+  int32_t ehrenfest;
+  int32_t n_obs_x;
+  const char* const* obs_x;
+  int32_t n_obs_p;
+  const char* const* obs_p;
+  int32_t n_terms;
+  const int32_t* term_slot;
+  const int32_t* term_kind;  /* AW_TERM_X / AW_TERM_P */
+  const int32_t* term_index; /* index into obs_x / obs_p */
+  const double* term_coef;
+  int32_t n_slots;
+} aw_config;
+
+/* library */
+int32_t aw_version(void);
+const char* aw_last_error(void);
+/* number of CUDA kernels this library has launched since load (all handles) */
+int64_t aw_launch_count(void);
+
+/* Timing of the handle's own launches with CUDA events (no counterpart in the
+ * reference, which has no timers).  aw_profile(h, 1) clears and starts
+ * recording; aw_profile_read fills, per launch class (0 row passes, 1 column
+ * passes, 2 expression kernels, 3 helper kernels), the summed device time in
+ * ms, the summed algorithmic HBM bytes and the launch count. */
+int aw_profile(aw_handle h, int32_t enable);
+int aw_profile_read(aw_handle h, double* ms4, double* bytes4, int64_t* launches4);
+
+/* Construction: replaces the __init__ of each propagator class
+ * (wigner_moyal_cuda_1d.py:17-327, wigner_bloch_cuda_1d.py:19-68,
+ * rho_vneumann_cuda_1d.py:22-335, rho_bloch_cuda_1d.py:20-68,
+ * schrodinger_wigner_cuda_1d.py:26-303): NVRTC compiles the expression
+ * strings (SourceModule in the reference), device buffers are allocated and
+ * the FFT twiddles and shear tables are built.  Bloch kinds also evaluate
+ * V_min and K_min (wigner_bloch_cuda_1d.py:70-92, rho_bloch_cuda_1d.py:70-98). */
+int aw_create(const aw_config* cfg, aw_handle* out);
+int aw_destroy(aw_handle h);
+int aw_stream(aw_handle h, void** stream);
+int aw_sync(aw_handle h);
+int aw_bloch_min(aw_handle h, double* v_min, double* k_min);
+
+/* Buffers: the device arrays the reference exposes as GPUArrays
+ * (self.rho, self.wignerfunction, self.wavefunction) and their .get(). */
+int aw_buffer(aw_handle h, int32_t which, void** dptr, int64_t* rows, int64_t* cols, int32_t* elem_bytes);
+/* copy in/out as interleaved complex128 host or device memory */
+int aw_set_buffer(aw_handle h, int32_t which, const void* src, int32_t src_on_device);
+int aw_get_buffer(aw_handle h, int32_t which, void* dst, int32_t dst_on_device);
+int aw_copy_buffer(aw_handle h, int32_t from, int32_t to);
+/* initial conditions given as a CUDA-C string (init kernels of
+ * wigner_moyal_cuda_1d.py:781-802, rho_vneumann_cuda_1d.py:773-794,
+ * schrodinger_wigner_cuda_1d.py:857-875) or a constant (GPUArray.fill) */
+int aw_fill_expr(aw_handle h, int32_t which, const char* expr);
+int aw_fill_const(aw_handle h, int32_t which, double re, double im);
+/* sum of a buffer (gpuarray.sum), trace of rho (skcuda linalg.trace),
+ * multiplication by a complex scalar (GPUArray /=) */
+int aw_sum(aw_handle h, int32_t which, double* re, double* im);
+int aw_trace(aw_handle h, double* re, double* im);
+int aw_scale(aw_handle h, int32_t which, double re, double im);
+
+/* Phase-space transforms.
+ *   WM/WB: aw_wigner2rho   = wigner_moyal_cuda_1d.py:422-469
+ *          aw_rho2wigner   = wigner_moyal_cuda_1d.py:471-538 (blackman != 0: :503-538)
+ *   VN/RB: aw_rho2wigner   = get_wignerfunction, rho_vneumann_cuda_1d.py:387-427 (normalised)
+ *   SW:    aw_rho2wigner   = get_wigner / get_wigner_blackman, schrodinger_wigner_cuda_1d.py:593-663
+ * aw_normalize_rho_wigner = wigner_moyal_cuda_1d.py:608-622 (WM/WB only). */
+int aw_wigner2rho(aw_handle h);
+int aw_rho2wigner(aw_handle h, int32_t blackman);
+int aw_normalize_rho_wigner(aw_handle h);
+
+/* Real-time propagation: `steps` repetitions of t += dt; single_step_propagation;
+ * normalisation; Ehrenfest observables -- wigner_moyal_cuda_1d.py:563-582,
+ * rho_vneumann_cuda_1d.py:429-448, schrodinger_wigner_cuda_1d.py:371-390.
+ * *t holds the time before the call and receives the time after it, accumulated
+ * step by step in FP64 exactly as the reference's `self.t += self.dt`. */
+int aw_propagate(aw_handle h, int64_t steps, double* t);
+/* Observables recorded by the last aw_propagate: rows x (n_slots + 2) doubles,
+ * columns = slots, purity, norm. */
+int aw_history(aw_handle h, double* out, int64_t max_rows, int64_t* rows, int32_t* cols);
+
+/* Expectation values.
+ *   WM/WB: Sum Re W f(X,P,t) dXdP            wigner_moyal_cuda_1d.py:329-347
+ *   SW:    Sum |psi|^2 f(X,P,t)              schrodinger_wigner_cuda_1d.py:392-410
+ *   VN/RB: Tr[... f3(x) g2(p) f1(x) rho] dX  rho_vneumann_cuda_1d.py:520-563
+ *          (ops = ordered tuple, NULL entries skip a factor) */
+int aw_average(aw_handle h, const char* expr, double t, double* out);
+int aw_average_ops(aw_handle h, const char* const* ops, int32_t n_ops, double t, double* out);
+/* purity: WM/WB 2 pi Sum W^2 dXdP (wm:349-354); VN/RB Sum |rho|^2 dX^2 (vn:565-579) */
+int aw_purity(aw_handle h, double* out);
+
+/* Imaginary time.
+ *   aw_bloch_step: one bloch_single_step_propagation including its
+ *   normalisation (wigner_bloch_cuda_1d.py:221-240, rho_bloch_cuda_1d.py:225-246)
+ *   followed by the recorded observables of one step: out[0..n_slots-1] slots,
+ *   out[n_slots] purity (may be NULL).
+ *   aw_gibbs: get_gibbs_state's loop (wigner_bloch_cuda_1d.py:119-155,
+ *   rho_bloch_cuda_1d.py:125-161): up to `steps` Bloch steps of size dbeta,
+ *   stopping after the first step whose purity is not below one.  *done
+ *   receives the number of steps taken, *purity the last purity. */
+int aw_bloch_step(aw_handle h, double dbeta, double* out);
+int aw_gibbs(aw_handle h, double dbeta, int64_t steps, int64_t* done, double* purity);
+
+/* Schrodinger imaginary time (schrodinger_wigner_cuda_1d.py:484-591):
+ * `steps` Bloch steps, each followed by renormalisation (project != 0:
+ * Gram-Schmidt against the stored stationary states instead). */
+int aw_sw_imag_steps(aw_handle h, int64_t steps, int32_t project);
+int aw_sw_store_state(aw_handle h);                 /* append psi to the stationary states */
+int aw_sw_get_state(aw_handle h, int32_t index, void* dst_host);
+int aw_sw_energy(aw_handle h, double t, double* out); /* get_energy, sw:461-482 */
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,138 @@
+"""Wigner-Moyal / Wigner-Bloch on the GPU against the oracle (plain complex128, 1e-10 relative L2)."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from _cases import WM_ANHARMONIC, WM_INIT, WM_STRONG_FIELD, e_field
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10  # plain complex128 form: relative L2 against the FP64 oracle
+
+
+def _pair(cls_gpu, cls_cpu, params, **extra):
+    from oracle.propagators import WignerMoyalOracle  # noqa: F401
+
+    g = cls_gpu(**params, **extra)
+    c = cls_cpu(**params)
+    return g, c
+
+
+def test_wigner2rho_rho2wigner_roundtrip():
+    from accuratewigner_gb300 import WignerMoyalCUDA1D
+    from oracle.propagators import WignerMoyalOracle
+
+    p = dict(WM_ANHARMONIC)
+    g = WignerMoyalCUDA1D(**p)
+    c = WignerMoyalOracle(**p)
+    g.set_wignerfunction(WM_INIT)
+    c.set_wignerfunction(WM_INIT)
+    assert rel_l2(g.rho.get(), c.rho) < TOL
+    g.rho2wigner()
+    c.rho2wigner()
+    assert rel_l2(g.wignerfunction.get(), c.wignerfunction) < TOL
+
+
+def test_propagate_ehrenfest_anharmonic():
+    from accuratewigner_gb300 import WignerMoyalCUDA1D
+    from oracle.propagators import WignerMoyalOracle
+
+    g = WignerMoyalCUDA1D(**WM_ANHARMONIC)
+    c = WignerMoyalOracle(**WM_ANHARMONIC)
+    g.set_wignerfunction(WM_INIT)
+    c.set_wignerfunction(WM_INIT)
+    g.propagate(25)
+    c.propagate(25)
+    assert g.t == c.t
+    assert rel_l2(g.wignerfunction.get(), c.wignerfunction) < TOL
+    assert rel_l2(g.rho.get(), c.rho) < TOL
+    for name in ("X_average", "X_average_RHS", "P_average", "P_average_RHS", "hamiltonian_average"):
+        assert len(getattr(g, name)) == 25
+        assert rel_l2(getattr(g, name), getattr(c, name)) < TOL, name
+    assert abs(g.get_purity() - c.get_purity()) < 1e-10
+    assert abs(g.get_average("X * P") - c.get_average("X * P")) < 1e-10
+
+
+def test_propagate_without_ehrenfest():
+    from accuratewigner_gb300 import WignerMoyalCUDA1D
+    from oracle.propagators import WignerMoyalOracle
+
+    p = {k: v for k, v in WM_ANHARMONIC.items() if k not in ("diff_K", "diff_V")}
+    g = WignerMoyalCUDA1D(**p)
+    c = WignerMoyalOracle(**p)
+    g.set_wignerfunction(WM_INIT)
+    c.set_wignerfunction(WM_INIT)
+    g.propagate(10)
+    c.propagate(10)
+    g.propagate(7)
+    c.propagate(7)
+    assert rel_l2(g.wignerfunction.get(), c.wignerfunction) < TOL
+    assert rel_l2(g.rho.get(), c.rho) < TOL
+
+
+def test_strong_field_time_dependent_with_absorber():
+    from accuratewigner_gb300 import WignerMoyalCUDA1D
+    from oracle.propagators import WignerMoyalOracle
+
+    p = dict(WM_STRONG_FIELD)
+    g = WignerMoyalCUDA1D(**p)
+    c = WignerMoyalOracle(**p, py_functions={"E": e_field})
+    init = "exp(-X * X - P * P) / M_PI"
+    g.set_wignerfunction(init)
+    c.set_wignerfunction(init)
+    g.propagate(30)
+    c.propagate(30)
+    assert rel_l2(g.wignerfunction.get(), c.wignerfunction) < TOL
+    for name in ("X_average", "P_average", "P_average_RHS", "hamiltonian_average"):
+        assert rel_l2(getattr(g, name), getattr(c, name)) < TOL, name
+
+
+def test_wigner_bloch_gibbs_matches_oracle_and_analytic():
+    from accuratewigner_gb300 import WignerBlochCUDA1D
+    from oracle.propagators import WignerBlochOracle
+
+    p = dict(t=0.0, dt=0.01, X_gridDIM=128, X_amplitude=10.0, P_gridDIM=128, P_amplitude=10.0, kT=0.5, omega=1.5,
+             K="0.5 * P * P", V="0.5 * omega * omega * X * X")
+    g = WignerBlochCUDA1D(**p)
+    c = WignerBlochOracle(**p)
+    assert g.V_min == c.V_min and g.K_min == c.K_min
+    Wg = g.get_gibbs_state().get()
+    Wc = c.get_gibbs_state()
+    assert g.gibbs_steps_done == c.gibbs_steps_done == 200
+    assert rel_l2(Wg, Wc) < TOL
+    assert rel_l2(g.rho.get(), c.rho) < TOL
+    exact = np.tanh(0.5 * 1.5 / 0.5) / np.pi * np.exp(
+        -2.0 * np.tanh(0.5 * 1.5 / 0.5) * 0.5 * (g.P ** 2 + 1.5 ** 2 * g.X ** 2) / 1.5)
+    assert np.abs(exact - Wg.real).max() * g.dXdP < 1e-6
+
+
+def test_wigner_bloch_purity_stop():
+    from accuratewigner_gb300 import WignerBlochCUDA1D
+    from oracle.propagators import WignerBlochOracle
+
+    # very low temperature: purity reaches 1 and the loop stops early (wb:144-153)
+    p = dict(t=0.0, dt=0.05, X_gridDIM=64, X_amplitude=6.0, P_gridDIM=64, P_amplitude=6.0, kT=0.005, dbeta=0.05,
+             K="0.5 * P * P", V="0.5 * X * X")
+    g = WignerBlochCUDA1D(**p)
+    c = WignerBlochOracle(**p)
+    Wg = g.get_gibbs_state().get()
+    Wc = c.get_gibbs_state()
+    n = g.get_dbeta_num_beta_steps(0.005, 0.05)[1]
+    # both stop once purity reaches one; the exact step depends on the last bits of the purity
+    assert g.gibbs_steps_done < n and c.gibbs_steps_done < n
+    assert g.get_purity() >= 1.0 - 1e-12
+    assert rel_l2(Wg, Wc) < 1e-6
+
+
+def test_wigner_bloch_ground_state():
+    from accuratewigner_gb300 import WignerBlochCUDA1D
+    from oracle.propagators import WignerBlochOracle
+
+    p = dict(t=0.0, dt=0.05, X_gridDIM=64, X_amplitude=6.0, P_gridDIM=64, P_amplitude=6.0, dbeta=0.05,
+             K="0.5 * P * P", V="0.5 * X * X")
+    g = WignerBlochCUDA1D(**p)
+    c = WignerBlochOracle(**p)
+    Wg = g.get_ground_state(abs_tol_purity=1e-8).get()
+    Wc = c.get_ground_state(abs_tol_purity=1e-8)
+    assert rel_l2(Wg, Wc) < 1e-8
+    assert abs(g.get_average(g.hamiltonian) - 0.5) < 1e-4
