@@ -8,5 +8,8 @@ the work runs in ``libawigner.so`` (C ABI in ``include/awigner.h``).
 """
 from .wigner_moyal_cuda_1d import WignerMoyalCUDA1D
 from .wigner_bloch_cuda_1d import WignerBlochCUDA1D
+from .rho_vneumann_cuda_1d import RhoVNeumannCUDA1D
+from .rho_bloch_cuda_1d import RhoBlochCUDA1D
+from .schrodinger_wigner_cuda_1d import SchrodingerWignerCUDA1D
 
-__all__ = ["WignerMoyalCUDA1D", "WignerBlochCUDA1D"]
+__all__ = ["WignerMoyalCUDA1D", "WignerBlochCUDA1D", "RhoVNeumannCUDA1D", "RhoBlochCUDA1D", "SchrodingerWignerCUDA1D"]

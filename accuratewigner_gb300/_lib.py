@@ -114,6 +114,7 @@ SIGNATURES = [
     ("aw_gibbs", c_int, [c_vp, c_dbl, c_i64, ctypes.POINTER(c_i64), ctypes.POINTER(c_dbl)]),
     ("aw_sw_imag_steps", c_int, [c_vp, c_i64, c_int]),
     ("aw_sw_store_state", c_int, [c_vp]),
+    ("aw_sw_clear_states", c_int, [c_vp]),
     ("aw_sw_get_state", c_int, [c_vp, c_int, c_vp]),
     ("aw_sw_energy", c_int, [c_vp, c_dbl, ctypes.POINTER(c_dbl)]),
 ]

@@ -156,6 +156,9 @@ struct aw_state_s {
   DevBuf part;                         // reduction partials (double2 x 1024)
   DevBuf blk_tabs;                     // Blackman tables
   int shx_lo_n = 0, shy_lo_n = 0;
+  DevBuf twist_hi, twist_lo;           // von Neumann momentum-diagonal twist exp(2 pi i k i / N) / N
+  int twist_lo_n = 0;
+  int sw_rows = 1;                     // Schrodinger: rows of the zero-padded psi tile
   int red_blocks = 0;                  // column blocks of the Wigner column pass
   int row_blocks = 0;                  // row blocks of the main row pass
   long long hist_rows = 0, hist_cap = 0;
@@ -297,7 +300,8 @@ static int make_twiddles(DevBuf& dst, int n, int f32) {
 // Two-level table of a bilinear phase exp(i alpha_line (q - npos/2)) * norm
 // for q = 0..npos-1, split as hi[q / lo] * lo[q % lo].
 static int make_shear(DevBuf& hi, DevBuf& lo, int* lo_n, const std::vector<double>& alpha, int npos, double norm,
-                      int f32) {
+                      int f32, double offset = -1.0) {
+  if (offset < 0) offset = 0.5 * npos;
   const int LO = npos < 32 ? npos : 32;
   const int nhi = npos / LO;
   const int lines = (int)alpha.size();
@@ -305,7 +309,7 @@ static int make_shear(DevBuf& hi, DevBuf& lo, int* lo_n, const std::vector<doubl
   for (int ln = 0; ln < lines; ++ln) {
     const double a = alpha[ln];
     for (int h = 0; h < nhi; ++h) {
-      const double ph = a * ((double)(h * LO) - 0.5 * npos);
+      const double ph = a * ((double)(h * LO) - offset);
       H[2 * ((size_t)ln * nhi + h)] = cos(ph) * norm;
       H[2 * ((size_t)ln * nhi + h) + 1] = sin(ph) * norm;
     }
@@ -318,6 +322,41 @@ static int make_shear(DevBuf& hi, DevBuf& lo, int* lo_n, const std::vector<doubl
   const size_t es = f32 ? 8 : 16;
   TRY(dalloc(hi, (size_t)lines * nhi * es));
   TRY(dalloc(lo, (size_t)lines * LO * es));
+  if (f32) {
+    std::vector<float> h2(H.begin(), H.end()), l2(L.begin(), L.end());
+    CK(cudaMemcpy(hi.p, h2.data(), h2.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(lo.p, l2.data(), l2.size() * 4, cudaMemcpyHostToDevice));
+  } else {
+    CK(cudaMemcpy(hi.p, H.data(), H.size() * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(lo.p, L.data(), L.size() * 8, cudaMemcpyHostToDevice));
+  }
+  *lo_n = LO;
+  return AW_OK;
+}
+
+// exp(2 pi i (line * q mod n) / n) / n split as hi[q / lo] * lo[q % lo], exact integer reduction
+static int make_twist(DevBuf& hi, DevBuf& lo, int* lo_n, int n, int f32) {
+  const int LO = n < 32 ? n : 32;
+  const int nhi = n / LO;
+  const long double PI = 3.141592653589793238462643383279502884L;
+  std::vector<double> H(2 * (size_t)n * nhi), L(2 * (size_t)n * LO);
+  for (long long ln = 0; ln < n; ++ln) {
+    for (int h = 0; h < nhi; ++h) {
+      const long long m = (ln * (long long)(h * LO)) % n;
+      const long double a = 2.0L * PI * (long double)m / (long double)n;
+      H[2 * ((size_t)ln * nhi + h)] = (double)(cosl(a) / n);
+      H[2 * ((size_t)ln * nhi + h) + 1] = (double)(sinl(a) / n);
+    }
+    for (int l = 0; l < LO; ++l) {
+      const long long m = (ln * (long long)l) % n;
+      const long double a = 2.0L * PI * (long double)m / (long double)n;
+      L[2 * ((size_t)ln * LO + l)] = (double)cosl(a);
+      L[2 * ((size_t)ln * LO + l) + 1] = (double)sinl(a);
+    }
+  }
+  const size_t es = f32 ? 8 : 16;
+  TRY(dalloc(hi, (size_t)n * nhi * es));
+  TRY(dalloc(lo, (size_t)n * LO * es));
   if (f32) {
     std::vector<float> h2(H.begin(), H.end()), l2(L.begin(), L.end());
     CK(cudaMemcpy(hi.p, h2.data(), h2.size() * 4, cudaMemcpyHostToDevice));
@@ -481,6 +520,8 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
     h->nr = 1;
     h->nc = N;
     h->wn = N;
+    h->sw_rows = aw_row_pass_lines(N, h->f32);
+    if (h->sw_rows <= 0) return fail(AW_E_ARG, "unsupported wave-function length %d", N);
   }
   const int maxn = h->kn.sw ? 8192 : 8192;
   if (h->nc < 64 || h->nc > maxn || (!h->kn.sw && (h->nr < 64 || h->nr > maxn)) || (h->wn && h->wn > 8192))
@@ -497,7 +538,7 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   if (h->kn.rotated) TRY(jit_kernel(h->lib, "aw_mask2d", &h->k_mask2d));
 
   // buffers
-  const size_t grid = (size_t)h->nr * h->nc;
+  const size_t grid = (size_t)(h->kn.sw ? h->sw_rows : h->nr) * h->nc;
   const size_t wgrid = h->kn.rotated ? grid : (size_t)h->wn * h->wn;
   TRY(dalloc(h->rho, grid * h->esz));
   TRY(dalloc(h->W, wgrid * h->esz));
@@ -558,6 +599,8 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
     TRY(make_shear(h->shx_hi, h->shx_lo, &h->shx_lo_n, ax, M, 1.0 / M, h->f32));
     TRY(make_shear(h->shy_hi, h->shy_lo, &h->shy_lo_n, ay, M, 1.0 / M, h->f32));
   }
+
+  if (h->kn.vn) TRY(make_twist(h->twist_hi, h->twist_lo, &h->twist_lo_n, h->nc, h->f32));
 
   // reduction scratch of the Wigner column pass
   const int wr = h->kn.rotated ? h->nr : h->wn, wc = h->kn.rotated ? h->nc : h->wn;
@@ -636,7 +679,7 @@ extern "C" int aw_create(const aw_config* cfg, aw_handle* out) {
 extern "C" int aw_destroy(aw_handle h) {
   if (!h) return AW_OK;
   if (h->st) cudaStreamSynchronize(h->st);
-  DevBuf* bufs[] = {&h->rho, &h->W, &h->snap, &h->tmp, &h->stage, &h->tw_r, &h->tw_c, &h->tw_w, &h->shx_hi,
+  DevBuf* bufs[] = {&h->twist_hi, &h->twist_lo, &h->rho, &h->W, &h->snap, &h->tmp, &h->stage, &h->tw_r, &h->tw_c, &h->tw_w, &h->shx_hi,
                     &h->shx_lo, &h->shy_hi, &h->shy_lo, &h->tabs, &h->maskx, &h->maskp, &h->red_line,
                     &h->red_cross, &h->red_sq, &h->rowsum, &h->diag, &h->abs2, &h->scal, &h->stop, &h->hist,
                     &h->terms, &h->part, &h->blk_tabs};
@@ -948,24 +991,47 @@ static int wigner_passes(aw_state_s* h, const WignerGrid& g, const void* first_i
   return AW_OK;
 }
 
-static int launch_finalize(aw_state_s* h, double t, double* hist_row, int stop_on_purity) {
-  const double* colsum = (const double*)h->red_line.p;
-  const double* rowpart = (const double*)h->red_cross.p;
-  int nparts = h->red_blocks;
-  const double* sqpart = (const double*)h->red_sq.p;
+struct FinalArgs {
+  const double* colsum;
+  int cstride;
+  int ncol;
+  const double* rowpart;
+  int nparts;
+  int nrow;
+  int proll;
+  const double* sqpart;
+  double dXdP;
+  double* inv;  // may be null
+  int pnorm_own;
+  int sqrt_norm;
+};
+
+static int launch_finalize_args(aw_state_s* h, const FinalArgs& f, double t, double* hist_row, int stop_on_purity) {
+  const double* colsum = f.colsum;
+  const double* rowpart = f.rowpart;
+  int nparts = f.nparts;
+  const double* sqpart = f.sqpart;
   double* rowsum = (double*)h->rowsum.p;
-  double* inv = dscal(h, 0);
+  double* inv = f.inv;
   int* stop = (int*)h->stop.p;
-  int ncol = h->nc, nrow = h->nr;
-  double dX = h->cfg.dX, dP = h->cfg.dP, dXdP = h->cfg.dXdP;
+  int ncol = f.ncol, nrow = f.nrow;
+  double dX = h->cfg.dX, dP = h->cfg.dP, dXdP = f.dXdP;
   const int* ts = (const int*)h->terms.p;
   const int* tk = ts + 64;
   const int* ti = ts + 128;
   const double* tc = (const double*)((const char*)h->terms.p + 64 * 3 * sizeof(int));
   int nterms = (int)h->tslot.size(), nslots = h->cfg.n_slots;
+  int cstride = f.cstride, proll = f.proll, pown = f.pnorm_own, sq = f.sqrt_norm;
   void* args[] = {&colsum, &rowpart, &nparts, &sqpart, &rowsum, &hist_row, &inv, &stop, &stop_on_purity, &t,
-                  &ncol, &nrow, &dX, &dP, &dXdP, &ts, &tk, &ti, &tc, &nterms, &nslots};
+                  &ncol, &nrow, &dX, &dP, &dXdP, &ts, &tk, &ti, &tc, &nterms, &nslots, &cstride, &proll, &pown, &sq};
   return hjit(h, h->k_final, dim3(1), dim3(256), args);
+}
+
+// rotated frame: marginals of W from the reducing column pass
+static int launch_finalize(aw_state_s* h, double t, double* hist_row, int stop_on_purity) {
+  FinalArgs f{(const double*)h->red_line.p, 1, h->nc, (const double*)h->red_cross.p, h->red_blocks, h->nr, 0,
+              (const double*)h->red_sq.p, h->cfg.dXdP, dscal(h, 0), 0, 0};
+  return launch_finalize_args(h, f, t, hist_row, stop_on_purity);
 }
 
 static int ensure_hist(aw_state_s* h, long long rows) {
@@ -1341,20 +1407,492 @@ extern "C" int aw_gibbs(aw_handle h, double dbeta, int64_t steps, int64_t* done,
 }
 
 // ============================================================================ von Neumann / rho-Bloch
-int vn_propagate(aw_state_s* h, long long steps, double* t) { return fail(AW_E_STATE, "von Neumann propagation not built yet"); }
-int vn_bloch_step(aw_state_s* h, double dbeta, double* out) { return fail(AW_E_STATE, "rho-Bloch not built yet"); }
-int vn_gibbs(aw_state_s* h, double dbeta, long long steps, long long* done, double* purity) {
-  return fail(AW_E_STATE, "rho-Bloch not built yet");
+// rho(x, x') on an N x N grid, the reference's RhoVNeumannCUDA1D / RhoBlochCUDA1D.
+// One step is the rotated-frame sequence with X / P tables (rho_vneumann_cuda_1d.py:450-468,
+// rho_bloch_cuda_1d.py:225-246) and the per-step trace normalisation folded into the next pass.
+struct VnPlan {
+  bool bloch;
+  double dbeta;
+  bool observables;    // per-step X / P diagonals and the user's averages
+  bool keep_rho;       // store rho_n (position representation) every step
+  int stop_on_purity;
+  int complex_trace;   // rho-Bloch divides by the complex trace (rho_bloch_cuda_1d.py:244)
+};
+
+static int vn_tables(aw_state_s* h, const VnPlan& p, double tn, bool kfirst) {
+  const aw_config& c = h->cfg;
+  if (p.bloch) {
+    TRY(build_tab(h, TAB_BV, 0, 1, c.t_initial, 0.0, -0.25 * p.dbeta, 0.0, 0.5 * h->V_min, 0, 0.0));
+    return build_tab(h, TAB_BK, 1, 1, c.t_initial, 0.0, -0.5 * p.dbeta, 0.0, 0.5 * h->K_min, 0, 0.0);
+  }
+  const double half = 0.5 * c.dt;
+  // expV: exp(-i dt/2 [V(X,t+dt/2) - V(X',t+dt/2)]) abs_boundary_x(X) abs_boundary_x(X')  (vn:754-770)
+  TRY(build_tab(h, TAB_V1, 0, 0, tn + half, 0.0, -half, 0.0, 0.0, c.absx_mode ? 1 : 0, 0.0));
+  // expK: exp(-i dt [K(P,t+dt/2) - K(P',t+dt/2)]) abs_boundary_p(P) abs_boundary_p(P')    (vn:733-745)
+  if (kfirst) TRY(build_tab(h, TAB_K, 1, 0, tn + half, 0.0, -c.dt, 0.0, 0.0, c.absp_mode ? 1 : 0, 0.0));
+  return AW_OK;
 }
-static int vn_get_wigner(aw_state_s* h, int blackman) { return fail(AW_E_STATE, "not built yet"); }
+
+// momentum-space diagonal of rho_n:  M_k = (1/N) Sum_i [fft1(S rho_n)]_ik exp(+2 pi i k i / N),
+// so that Tr[g(p) rho] dX = Sum_k g(P_k) M_k dX (the p branch of get_average, vn:548-561)
+static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::vector<double>& times, double* hist,
+                  int hist_stride) {
+  const aw_config& c = h->cfg;
+  const bool vdep = !p.bloch && c.v_time_dependent;
+  const bool kdep = !p.bloch && c.k_time_dependent;
+  const int N = h->nc;
+  KL(aw_k_set2(dscal(h, 0), 1.0, 0.0, h->st));
+  if (p.stop_on_purity) CK(cudaMemsetAsync(h->stop.p, 0, sizeof(int), h->st));
+  const int* stop = p.stop_on_purity ? (const int*)h->stop.p : nullptr;
+  const int row_blocks = aw_row_pass_blocks(h->nr, h->nc, h->f32);
+  const int vslot = p.bloch ? TAB_BV : TAB_V1;
+  const int kslot = p.bloch ? TAB_BK : TAB_K;
+  // for time-dependent V the next step's kick needs its own table
+  if (!vdep) TRY(vn_tables(h, p, times[1], true));
+  {
+    if (vdep) TRY(vn_tables(h, p, times[1], !kdep));
+    AwPassArgs a = pnone(h);
+    a.in = a.out = h->rho.p;
+    a.f2 = ftab(h, vslot);
+    a.f2.sign = 1;
+    a.d2 = +1;
+    a.stop = stop;
+    TRY(row_pass(h, a, h->tw_r));
+  }
+  for (long long n = 1; n <= steps; ++n) {
+    const bool last = n == steps;
+    {
+      if (kdep) TRY(build_tab(h, TAB_K, 1, 0, times[n] + 0.5 * c.dt, 0.0, -c.dt, 0.0, 0.0, c.absp_mode ? 1 : 0, 0.0));
+      AwPassArgs a = pnone(h);
+      a.in = a.out = h->rho.p;
+      a.f0 = fnone();
+      a.f0.scale_ptr = dscal(h, 0);
+      a.f0.active = 1;
+      a.d1 = -1;
+      a.f1 = ftab(h, kslot);
+      a.d2 = +1;
+      a.stop = stop;
+      TRY(col_pass(h, a, h->tw_c));
+    }
+    {
+      if (vdep) {
+        // tables at t_n and at t_{n+1} for the fused kicks
+        TRY(build_tab(h, TAB_V1, 0, 0, times[n] + 0.5 * c.dt, 0.0, -0.5 * c.dt, 0.0, 0.0, c.absx_mode ? 1 : 0, 0.0));
+        if (!last)
+          TRY(build_tab(h, TAB_V1B, 0, 0, times[n + 1] + 0.5 * c.dt, 0.0, -0.5 * c.dt, 0.0, 0.0, c.absx_mode ? 1 : 0, 0.0));
+      }
+      AwPassArgs a = pnone(h);
+      a.in = a.out = h->rho.p;
+      a.d1 = -1;
+      a.f1 = ftab(h, vslot);
+      a.diag_out = (double2*)h->diag.p;
+      if (p.stop_on_purity || p.bloch) a.red_abs2 = (double*)h->abs2.p;
+      if (p.keep_rho) {
+        a.mid_out = h->snap.p;
+        a.mid_sign = 1;
+      }
+      if (p.observables) {
+        a.br_out = h->tmp.p;
+        a.br_d1 = +1;
+        a.fbr = fnone();
+        a.fbr.sh_hi = h->twist_hi.p;
+        a.fbr.sh_lo = h->twist_lo.p;
+        a.fbr.sh_lo_n = h->twist_lo_n;
+        a.fbr.active = 1;
+      }
+      if (!last) {
+        a.f2 = ftab(h, vdep ? TAB_V1B : vslot);
+        a.d2 = +1;
+      } else {
+        a.f2 = fsign();
+      }
+      a.stop = stop;
+      TRY(row_pass(h, a, h->tw_r));
+    }
+    double* hrow = hist ? hist + (size_t)(n - 1) * hist_stride : nullptr;
+    if (p.observables) {
+      // column sums of the twisted branch: Re M_k
+      AwPassArgs a = pnone(h);
+      a.in = h->tmp.p;
+      a.red_line = (double*)h->red_line.p;
+      a.stop = stop;
+      TRY(col_pass(h, a, h->tw_c));
+    }
+    if (p.bloch || !p.observables) {
+      KL(aw_k_trace_finalize((const double2*)h->diag.p, N, (const double*)h->abs2.p, row_blocks, c.dX,
+                             p.complex_trace, dscal(h, 0), p.observables ? nullptr : hrow, (int*)h->stop.p,
+                             p.stop_on_purity, h->st));
+    }
+    if (p.observables) {
+      FinalArgs f{(const double*)h->diag.p, 2, N, (const double*)h->red_line.p, 1, N, 0, nullptr, c.dX,
+                  p.bloch ? nullptr : dscal(h, 0), 0, 0};
+      TRY(launch_finalize_args(h, f, times[n], hrow, 0));
+    }
+  }
+  return AW_OK;
+}
+
+int vn_propagate(aw_state_s* h, long long steps, double* t) {
+  const aw_config& c = h->cfg;
+  std::vector<double> times(steps + 2);
+  times[0] = *t;
+  for (long long n = 1; n <= steps + 1; ++n) times[n] = times[n - 1] + c.dt;
+  TRY(ensure_hist(h, steps + 1));
+  if (steps == 0) return AW_OK;
+  VnPlan p{false, 0.0, c.ehrenfest != 0, false, 0, 0};
+  TRY(vn_run(h, p, steps, times, c.ehrenfest ? (double*)h->hist.p : nullptr, h->hist_cols));
+  KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
+  h->hist_rows = c.ehrenfest ? steps : 0;
+  *t = times[steps];
+  return AW_OK;
+}
+
+int vn_bloch_step(aw_state_s* h, double dbeta, double* out) {
+  TRY(ensure_hist(h, 2));
+  CK(cudaMemsetAsync(h->hist.p, 0, 2 * (size_t)h->hist_cols * 8, h->st));
+  const bool obs = h->cfg.n_slots > 0;
+  VnPlan p{true, dbeta, obs, false, 0, 1};
+  std::vector<double> times(3, 0.0);
+  // observables go to row 0, the trace finalize (purity, trace) to row 1
+  TRY(vn_run(h, p, 1, times, (double*)h->hist.p, h->hist_cols));
+  if (obs)
+    KL(aw_k_trace_finalize((const double2*)h->diag.p, h->nc, (const double*)h->abs2.p,
+                           aw_row_pass_blocks(h->nr, h->nc, h->f32), h->cfg.dX, 1, dscal(h, 2),
+                           (double*)h->hist.p + h->hist_cols, nullptr, 0, h->st));
+  KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
+  if (out) {
+    std::vector<double> hh(2 * (size_t)h->hist_cols);
+    CK(cudaMemcpyAsync(hh.data(), h->hist.p, hh.size() * 8, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    const int ns = h->cfg.n_slots;
+    for (int k = 0; k < ns; ++k) out[k] = hh[k];
+    out[ns] = obs ? hh[h->hist_cols] : hh[0];  // purity
+    out[ns + 1] = obs ? hh[h->hist_cols + 1] : hh[1];
+  }
+  CK(cudaStreamSynchronize(h->st));
+  return AW_OK;
+}
+
+int vn_gibbs(aw_state_s* h, double dbeta, long long steps, long long* done, double* purity) {
+  *done = 0;
+  if (steps <= 0) return AW_OK;
+  TRY(ensure_hist(h, steps + 1));
+  const int hc = 3;
+  TRY(dalloc(h->hist, (size_t)(steps + 1) * hc * 8));
+  CK(cudaMemsetAsync(h->hist.p, 0, (size_t)(steps + 1) * hc * 8, h->st));
+  TRY(dalloc(h->snap, (size_t)h->nr * h->nc * h->esz));
+  VnPlan p{true, dbeta, false, true, 1, 1};
+  std::vector<double> times(steps + 2, 0.0);
+  TRY(vn_run(h, p, steps, times, (double*)h->hist.p, hc));
+  std::vector<double> hh((size_t)steps * hc);
+  CK(cudaMemcpyAsync(hh.data(), h->hist.p, hh.size() * 8, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  long long ran = 0;
+  for (long long n = 0; n < steps; ++n) {
+    if (hh[(size_t)n * hc + 1] == 0.0) break;
+    ran = n + 1;
+  }
+  *done = ran;
+  if (purity && ran > 0) *purity = hh[(size_t)(ran - 1) * hc];
+  CK(cudaMemcpyAsync(h->rho.p, h->snap.p, (size_t)h->nr * h->nc * h->esz, cudaMemcpyDeviceToDevice, h->st));
+  KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->hist_rows = 0;
+  return AW_OK;
+}
+
+// get_wignerfunction (rho_vneumann_cuda_1d.py:387-427): embed rho in the centre of a zeroed
+// (2N)^2 grid, sign flip, three shears, ifft0, sign flip, normalise by Re Sum W dXdP_wigner
+static int vn_get_wigner(aw_state_s* h, int blackman) {
+  const int N = h->nc, M = h->wn, pad = N / 2;
+  KL(aw_k_embed(h->rho.p, h->f32, N, h->W.p, M, pad, h->st));
+  if (blackman) TRY(ensure_blackman(h, M, M));
+  WignerGrid g{h->W.p, M, M, &h->tw_w, &h->tw_w};
+  TRY(wigner_passes(h, g, h->W.p, fsign(), blackman != 0, false, true));
+  double s[2];
+  TRY(dsum(h, h->W.p, (long long)M * M, 0, 0, s));
+  KL(aw_k_scale(h->W.p, h->f32, (long long)M * M, 1.0 / (s[0] * h->cfg.dXdP), 0.0, nullptr, h->st));
+  return AW_OK;
+}
+
 extern "C" int aw_average_ops(aw_handle h, const char* const* ops, int32_t n_ops, double t, double* out) {
-  return fail(AW_E_STATE, "not built yet");
+  if (!h || !out) return fail(AW_E_ARG, "null argument");
+  if (!h->kn.vn) return fail(AW_E_STATE, "ordered operator averages are defined for density matrices");
+  const long long n = (long long)h->nr * h->nc;
+  CK(cudaMemcpyAsync(h->tmp.p, h->rho.p, n * h->esz, cudaMemcpyDeviceToDevice, h->st));
+  bool is_x = false;
+  for (int k = 0; k < n_ops; ++k) {
+    is_x = !is_x;
+    if (!ops[k] || !ops[k][0]) continue;
+    cudaKernel_t kern;
+    TRY(get_obs_kernel(h, ops[k], &kern));
+    void* buf = h->tmp.p;
+    int f32 = h->f32, nr = h->nr, nc = h->nc;
+    double* unused = nullptr;
+    double dX = h->cfg.dX, dP = h->cfg.dP;
+    void* args[] = {&buf, &f32, &t, &unused, &nr, &nc, &dX, &dP};
+    if (is_x) {
+      TRY(hjit(h, kern, dim3((nc + 127) / 128, nr), dim3(128), args));
+    } else {
+      // sign flip, fft1, / N, observable, ifft1, sign flip (rho_vneumann_cuda_1d.py:549-561)
+      AwPassArgs a = pnone(h);
+      a.in = a.out = h->tmp.p;
+      a.f0 = fsign();
+      a.d1 = +1;
+      a.f1 = fnone();
+      a.f1.scale = 1.0 / nc;
+      a.f1.active = 1;
+      TRY(row_pass(h, a, h->tw_r));
+      TRY(hjit(h, kern, dim3((nc + 127) / 128, nr), dim3(128), args));
+      a = pnone(h);
+      a.in = a.out = h->tmp.p;
+      a.d1 = -1;
+      a.f3 = fsign();
+      TRY(row_pass(h, a, h->tw_r));
+    }
+  }
+  double s[2];
+  TRY(dsum(h, h->tmp.p, h->nr, 3, h->nc + 1, s));
+  *out = s[0] * h->cfg.dX;
+  return AW_OK;
 }
 
 // ============================================================================ Schrodinger
-int sw_propagate(aw_state_s* h, long long steps, double* t) { return fail(AW_E_STATE, "Schrodinger not built yet"); }
-static int sw_get_wigner(aw_state_s* h, int blackman) { return fail(AW_E_STATE, "not built yet"); }
-extern "C" int aw_sw_imag_steps(aw_handle h, int64_t steps, int32_t project) { return fail(AW_E_STATE, "not built yet"); }
-extern "C" int aw_sw_store_state(aw_handle h) { return fail(AW_E_STATE, "not built yet"); }
-extern "C" int aw_sw_get_state(aw_handle h, int32_t index, void* dst_host) { return fail(AW_E_STATE, "not built yet"); }
-extern "C" int aw_sw_energy(aw_handle h, double t, double* out) { return fail(AW_E_STATE, "not built yet"); }
+// psi on N points, stored as row 0 of a small zero-padded tile so that the row pass
+// kernels apply unchanged.  One step (schrodinger_wigner_cuda_1d.py:356-390):
+//   expV(t) -> fft -> expK(t) -> ifft -> expV(t) -> [Ehrenfest] -> psi /= ||psi|| sqrt(dX)
+static int sw_tables(aw_state_s* h, double t) {
+  const aw_config& c = h->cfg;
+  TRY(build_tab(h, TAB_V1, 0, 0, t, 0.0, -0.5 * c.dt, 0.0, 0.0, c.absx_mode ? 1 : 0, t));
+  return build_tab(h, TAB_K, 1, 0, t, 0.0, -c.dt, 0.0, 0.0, c.absp_mode ? 1 : 0, t);
+}
+
+static AwPassArgs sw_args(aw_state_s* h) {
+  AwPassArgs a = pnone(h);
+  a.nrows = h->sw_rows;
+  a.ncols = h->nc;
+  return a;
+}
+
+static int sw_finalize(aw_state_s* h, double t, double* hrow) {
+  const int N = h->nc;
+  double* xm = (double*)h->red_line.p;    // |psi_j|^2
+  double* pmar = (double*)h->red_cross.p; // |(fft psi)_k|^2
+  KL(aw_k_abs2(h->W.p, h->f32, N, xm, h->st));
+  KL(aw_k_abs2(h->tmp.p, h->f32, N, pmar, h->st));
+  FinalArgs f{xm, 1, N, pmar, 1, N, N / 2, nullptr, h->cfg.dX, dscal(h, 0), 1, 1};
+  return launch_finalize_args(h, f, t, hrow, 0);
+}
+
+int sw_propagate(aw_state_s* h, long long steps, double* t) {
+  const aw_config& c = h->cfg;
+  std::vector<double> times(steps + 2);
+  times[0] = *t;
+  for (long long n = 1; n <= steps + 1; ++n) times[n] = times[n - 1] + c.dt;
+  TRY(ensure_hist(h, steps + 1));
+  if (steps == 0) return AW_OK;
+  const bool tdep = c.v_time_dependent || c.k_time_dependent || c.absx_mode == 2 || c.absp_mode == 2;
+  KL(aw_k_set2(dscal(h, 0), 1.0, 0.0, h->st));
+  if (!tdep) TRY(sw_tables(h, times[1]));
+  const int nb = aw_row_pass_blocks(h->sw_rows, h->nc, h->f32);
+  for (long long n = 1; n <= steps; ++n) {
+    if (tdep) TRY(sw_tables(h, times[n]));
+    AwPassArgs a = sw_args(h);
+    a.in = h->rho.p;
+    a.out = c.ehrenfest ? h->W.p : h->rho.p;
+    a.f0 = ftab(h, TAB_V1);
+    a.f0.row_tab = nullptr;
+    a.f0.scale_ptr = dscal(h, 0);
+    a.d1 = +1;
+    a.f1 = ftab(h, TAB_K);
+    a.f1.row_tab = nullptr;
+    a.d2 = -1;
+    a.f3 = ftab(h, TAB_V1);
+    a.f3.row_tab = nullptr;
+    if (!c.ehrenfest) {
+      a.red_abs2 = (double*)h->abs2.p;
+      a.abs2_end = 1;
+    } else {
+      // psi' -> W buffer; its momentum representation -> tmp
+      a.br_out = nullptr;
+    }
+    TRY(row_pass(h, a, h->tw_r));
+    if (c.ehrenfest) {
+      AwPassArgs b = sw_args(h);
+      b.in = h->W.p;
+      b.out = h->tmp.p;
+      b.d1 = +1;
+      TRY(row_pass(h, b, h->tw_r));
+      TRY(sw_finalize(h, times[n], (double*)h->hist.p + (size_t)(n - 1) * h->hist_cols));
+      CK(cudaMemcpyAsync(h->rho.p, h->W.p, (size_t)h->sw_rows * h->nc * h->esz, cudaMemcpyDeviceToDevice, h->st));
+    } else {
+      KL(aw_k_norm_finalize((const double*)h->abs2.p, nb, c.dX, dscal(h, 0), nullptr, h->st));
+    }
+  }
+  KL(aw_k_scale(h->rho.p, h->f32, h->nc, 1.0, 0.0, dscal(h, 0), h->st));
+  h->hist_rows = c.ehrenfest ? steps : 0;
+  *t = times[steps];
+  return AW_OK;
+}
+
+// get_wigner / get_wigner_blackman (schrodinger_wigner_cuda_1d.py:593-663)
+static int sw_get_wigner(aw_state_s* h, int blackman) {
+  const int N = h->nc;
+  KL(aw_k_psi2rho(h->rho.p, h->f32, N, h->W.p, h->st));
+  if (blackman) TRY(ensure_blackman(h, N, N));
+  void* bcol = blackman ? h->blk_tabs.p : nullptr;
+  void* brow = blackman ? (char*)h->blk_tabs.p + (size_t)N * h->esz : nullptr;
+  AwFactor shx = fshear_x(h), shy = fshear_y(h);
+  shx.sh_roll = N / 2;
+  shy.sh_roll = N / 2;
+  AwPassArgs a = pnone(h);
+  a.nrows = a.ncols = N;
+  a.in = a.out = h->W.p;
+  if (blackman) { a.f0.col_tab = bcol; a.f0.active = 1; }
+  a.d1 = +1; a.f1 = shx; a.d2 = -1;
+  TRY(row_pass(h, a, h->tw_w));
+  a = pnone(h);
+  a.nrows = a.ncols = N;
+  a.in = a.out = h->W.p;
+  if (blackman) { a.f0.row_tab = brow; a.f0.active = 1; }
+  a.d1 = +1; a.f1 = shy; a.d2 = -1;
+  TRY(col_pass(h, a, h->tw_w));
+  a = pnone(h);
+  a.nrows = a.ncols = N;
+  a.in = a.out = h->W.p;
+  if (blackman) { a.f0.col_tab = bcol; a.f0.active = 1; }
+  a.d1 = +1; a.f1 = shx; a.d2 = -1;
+  TRY(row_pass(h, a, h->tw_w));
+  a = pnone(h);
+  a.nrows = a.ncols = N;
+  a.in = a.out = h->W.p;
+  a.f0 = fnone();
+  a.f0.sign = 2;
+  a.f0.active = 1;
+  if (blackman) a.f0.row_tab = brow;
+  a.d1 = -1;
+  a.f3 = fnone();
+  a.f3.sign = 2;
+  a.f3.active = 1;
+  TRY(col_pass(h, a, h->tw_w));
+  double s[2];
+  TRY(dsum(h, h->W.p, (long long)N * N, 0, 0, s));
+  KL(aw_k_scale(h->W.p, h->f32, (long long)N * N, 1.0 / (s[0] * h->cfg.dXdP), 0.0, nullptr, h->st));
+  return AW_OK;
+}
+
+// imaginary-time steps (set_ground_state / get_stationary_states, sw:484-591)
+extern "C" int aw_sw_imag_steps(aw_handle h, int64_t steps, int32_t project) {
+  if (!h) return fail(AW_E_ARG, "null handle");
+  if (!h->kn.sw) return fail(AW_E_STATE, "imaginary-time wave-function steps need the Schrodinger propagator");
+  const aw_config& c = h->cfg;
+  // bloch_expV = exp(-dt/2 V(X, t_initial)), bloch_expK = exp(-dt K(P, t_initial))  (sw:834-854)
+  TRY(build_tab(h, TAB_BV, 0, 1, c.t_initial, 0.0, -0.5 * c.dt, 0.0, 0.0, 0, 0.0));
+  TRY(build_tab(h, TAB_BK, 1, 1, c.t_initial, 0.0, -c.dt, 0.0, 0.0, 0, 0.0));
+  const int nb = aw_row_pass_blocks(h->sw_rows, h->nc, h->f32);
+  const int N = h->nc;
+  for (long long n = 0; n < steps; ++n) {
+    AwPassArgs a = sw_args(h);
+    a.in = a.out = h->rho.p;
+    a.f0 = ftab(h, TAB_BV);
+    a.f0.row_tab = nullptr;
+    a.d1 = +1;
+    a.f1 = ftab(h, TAB_BK);
+    a.f1.row_tab = nullptr;
+    a.d2 = -1;
+    a.f3 = ftab(h, TAB_BV);
+    a.f3.row_tab = nullptr;
+    if (!project) {
+      a.red_abs2 = (double*)h->abs2.p;
+      a.abs2_end = 1;
+    }
+    TRY(row_pass(h, a, h->tw_r));
+    if (!project) {
+      // psi /= norm(psi) sqrt(dX)
+      KL(aw_k_norm_finalize((const double*)h->abs2.p, nb, c.dX, dscal(h, 0), nullptr, h->st));
+      KL(aw_k_scale(h->rho.p, h->f32, N, 1.0, 0.0, dscal(h, 0), h->st));
+    } else {
+      // projectout_stationary_states (sw:505-550): normalise, subtract projections, normalise
+      double s[2];
+      TRY(dsum(h, h->rho.p, N, 2, 0, s));
+      KL(aw_k_scale(h->rho.p, h->f32, N, 1.0 / sqrt(s[0]), 0.0, nullptr, h->st));
+      std::vector<double2> proj(h->sw_states.size());
+      for (size_t q = 0; q < h->sw_states.size(); ++q) {
+        // <phi_q | psi>
+        KL(aw_k_vdot(h->sw_states[q].p, h->rho.p, h->f32, N, (double2*)h->part.p, 256, h->st));
+        std::vector<double2> hp(256);
+        CK(cudaMemcpyAsync(hp.data(), h->part.p, 256 * sizeof(double2), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        double re = 0, im = 0;
+        for (auto& v : hp) { re += v.x; im += v.y; }
+        proj[q] = make_double2(re, im);
+      }
+      for (size_t q = 0; q < h->sw_states.size(); ++q)
+        KL(aw_k_axpy(h->rho.p, h->sw_states[q].p, h->f32, N, -proj[q].x, -proj[q].y, h->st));
+      TRY(dsum(h, h->rho.p, N, 2, 0, s));
+      KL(aw_k_scale(h->rho.p, h->f32, N, 1.0 / sqrt(s[0]), 0.0, nullptr, h->st));
+    }
+  }
+  CK(cudaStreamSynchronize(h->st));
+  return AW_OK;
+}
+
+extern "C" int aw_sw_store_state(aw_handle h) {
+  if (!h || !h->kn.sw) return fail(AW_E_STATE, "stationary states need the Schrodinger propagator");
+  DevBuf b;
+  TRY(dalloc(b, (size_t)h->nc * h->esz));
+  CK(cudaMemcpyAsync(b.p, h->rho.p, (size_t)h->nc * h->esz, cudaMemcpyDeviceToDevice, h->st));
+  h->sw_states.push_back(b);
+  return AW_OK;
+}
+
+extern "C" int aw_sw_clear_states(aw_handle h) {
+  if (!h) return fail(AW_E_ARG, "null handle");
+  for (DevBuf& b : h->sw_states) dfree(b);
+  h->sw_states.clear();
+  return AW_OK;
+}
+
+extern "C" int aw_sw_get_state(aw_handle h, int32_t index, void* dst_host) {
+  if (!h || !dst_host) return fail(AW_E_ARG, "null argument");
+  if (index < 0 || index >= (int)h->sw_states.size()) return fail(AW_E_ARG, "no stationary state %d", index);
+  const void* src = h->sw_states[index].p;
+  if (h->f32) {
+    KL(aw_k_convert(src, 1, h->tmp.p, 0, h->nc, h->st));
+    src = h->tmp.p;
+  }
+  CK(cudaMemcpyAsync(dst_host, src, (size_t)h->nc * 16, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return AW_OK;
+}
+
+// get_energy (sw:461-482): <V> over |psi|^2 / Sum |psi|^2 plus <K> over |fft psi|^2 / Sum |fft psi|^2
+extern "C" int aw_sw_energy(aw_handle h, double t, double* out) {
+  if (!h || !out) return fail(AW_E_ARG, "null argument");
+  if (!h->kn.sw) return fail(AW_E_STATE, "get_energy needs the Schrodinger propagator");
+  double v, k, n1[2], n2[2];
+  TRY(dsum(h, h->rho.p, h->nc, 2, 0, n1));
+  TRY(aw_average(h, h->V.c_str(), t, &v));
+  AwPassArgs a = sw_args(h);
+  a.in = h->rho.p;
+  a.out = h->tmp.p;
+  a.d1 = +1;
+  TRY(row_pass(h, a, h->tw_r));
+  TRY(dsum(h, h->tmp.p, h->nc, 2, 0, n2));
+  // average of K over the momentum representation held in tmp
+  cudaKernel_t kern;
+  TRY(get_obs_kernel(h, h->K.c_str(), &kern));
+  const void* src = h->tmp.p;
+  int f32 = h->f32, nr = 1, nc = h->nc;
+  double* part = (double*)h->part.p;
+  double dX = h->cfg.dX, dP = h->cfg.dP;
+  void* args[] = {&src, &f32, &t, &part, &nr, &nc, &dX, &dP};
+  TRY(hjit(h, kern, dim3(256), dim3(256), args));
+  std::vector<double> hp(256);
+  CK(cudaMemcpyAsync(hp.data(), part, 256 * 8, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  k = 0;
+  for (double x : hp) k += x;
+  *out = v / n1[0] + k / n2[0];
+  return AW_OK;
+}

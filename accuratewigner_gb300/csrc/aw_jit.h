@@ -169,17 +169,24 @@ extern "C" __global__ void aw_values(double* aw_out, int aw_fn, int aw_n, double
   aw_out[aw_k] = aw_fn == 0 ? V(aw_x, aw_t) : K(aw_x, aw_t);
 }
 
-// Per-step observables from the marginals of the (unnormalised) Wigner
-// function: colsum[j] = Sum_i Re W[i][j], rowpart[p][i] = partial row sums.
-// Writes slots (sums of X-only and P-only averages, normalised as
-// wigner_moyal_cuda_1d.py:608-622 normalises W), the purity 2 pi Sum W^2 dXdP
-// of the normalised W, the norm, and 1 / norm for the next pass.
+// Per-step observables from the marginals of the state.
+//   aw_colsum[j * aw_cstride]: X-marginal on x_j = dX (j - ncol/2)
+//   aw_rowpart[p][i] (p < aw_nparts): partial P-marginals on p_i = dP (((i + aw_proll) mod nrow) - nrow/2)
+// For the rotated frame these are the column and row sums of Re W; for the
+// density matrix the diagonal in x and in p; for the wave function |psi|^2
+// and |fft psi|^2.  Slots are sums of X-only / P-only averages normalised by
+// norm = Sum colsum * aw_dXdP (P-terms by their own marginal when
+// aw_pnorm_own), as wigner_moyal_cuda_1d.py:608-622 normalises W.  The kernel
+// also writes the purity 2 pi Sum W^2 dXdP / norm^2 (rotated frame), the norm,
+// and the factor the next pass applies: 1 / norm (or 1 / sqrt(norm) when
+// aw_sqrt_norm, for a wave function).
 extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw_rowpart, int aw_nparts,
                                        const double* aw_sqpart, double* aw_rowsum, double* aw_hist,
                                        double* aw_inv_norm, int* aw_stop, int aw_stop_on_purity, double t,
                                        int aw_ncol, int aw_nrow, double aw_dX, double aw_dP, double aw_dXdP,
                                        const int* aw_tslot, const int* aw_tkind, const int* aw_tidx,
-                                       const double* aw_tcoef, int aw_nterms, int aw_nslots) {
+                                       const double* aw_tcoef, int aw_nterms, int aw_nslots,
+                                       int aw_cstride, int aw_proll, int aw_pnorm_own, int aw_sqrt_norm) {
   __shared__ double aw_red[256];
   __shared__ double aw_tv[64];
   if (aw_stop && *aw_stop) return;
@@ -192,10 +199,14 @@ extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw
   }
   __syncthreads();
   double aw_s = 0.0;
-  for (int aw_j = aw_t; aw_j < aw_ncol; aw_j += aw_nt) aw_s += aw_colsum[aw_j];
+  for (int aw_j = aw_t; aw_j < aw_ncol; aw_j += aw_nt) aw_s += aw_colsum[(long long)aw_j * aw_cstride];
   const double aw_norm_raw = aw_block_sum(aw_s, aw_red);
   aw_s = 0.0;
-  for (int aw_p = aw_t; aw_p < aw_nparts; aw_p += aw_nt) aw_s += aw_sqpart[aw_p];
+  for (int aw_i = aw_t; aw_i < aw_nrow; aw_i += aw_nt) aw_s += aw_rowsum[aw_i];
+  const double aw_pnorm_raw = aw_block_sum(aw_s, aw_red);
+  aw_s = 0.0;
+  if (aw_sqpart)
+    for (int aw_p = aw_t; aw_p < aw_nparts; aw_p += aw_nt) aw_s += aw_sqpart[aw_p];
   const double aw_sq = aw_block_sum(aw_s, aw_red);
   for (int aw_k = 0; aw_k < aw_nterms && aw_k < 64; ++aw_k) {
     aw_s = 0.0;
@@ -203,11 +214,11 @@ extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw
     if (aw_tkind[aw_k] == 0) {
       for (int aw_j = aw_t; aw_j < aw_ncol; aw_j += aw_nt) {
         const double X = aw_dX * ((aw_size_t)aw_j - 0.5 * aw_ncol);
-        aw_s += aw_colsum[aw_j] * aw_obs_x(aw_idx, X, t);
+        aw_s += aw_colsum[(long long)aw_j * aw_cstride] * aw_obs_x(aw_idx, X, t);
       }
     } else {
       for (int aw_i = aw_t; aw_i < aw_nrow; aw_i += aw_nt) {
-        const double P = aw_dP * ((aw_size_t)aw_i - 0.5 * aw_nrow);
+        const double P = aw_dP * ((aw_size_t)((aw_i + aw_proll) % aw_nrow) - 0.5 * aw_nrow);
         aw_s += aw_rowsum[aw_i] * aw_obs_p(aw_idx, P, t);
       }
     }
@@ -217,12 +228,17 @@ extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw
   if (aw_t == 0) {
     const double aw_norm = aw_norm_raw * aw_dXdP;
     for (int aw_q = 0; aw_q < aw_nslots; ++aw_q) aw_hist[aw_q] = 0.0;
-    for (int aw_k = 0; aw_k < aw_nterms && aw_k < 64; ++aw_k)
-      aw_hist[aw_tslot[aw_k]] += aw_tcoef[aw_k] * (aw_tv[aw_k] * aw_dXdP / aw_norm);
+    for (int aw_k = 0; aw_k < aw_nterms && aw_k < 64; ++aw_k) {
+      const bool aw_own = aw_pnorm_own && aw_tkind[aw_k] == 1;
+      aw_hist[aw_tslot[aw_k]] += aw_tcoef[aw_k] * (aw_own ? aw_tv[aw_k] / aw_pnorm_raw : aw_tv[aw_k] * aw_dXdP / aw_norm);
+    }
     const double aw_purity = 2.0 * M_PI * aw_sq * aw_dXdP / (aw_norm * aw_norm);
     aw_hist[aw_nslots] = aw_purity;
     aw_hist[aw_nslots + 1] = aw_norm;
-    *aw_inv_norm = 1.0 / aw_norm;
+    if (aw_inv_norm) {
+      aw_inv_norm[0] = aw_sqrt_norm ? 1.0 / sqrt(aw_norm) : 1.0 / aw_norm;
+      aw_inv_norm[1] = 0.0;
+    }
     if (aw_stop && aw_stop_on_purity && !(aw_purity < 1.0)) *aw_stop = 1;
   }
 }

@@ -77,7 +77,7 @@ __device__ __forceinline__ void apply_factor(V* s, const AwFactor& f, int line0,
     const int j = Tile::IS_ROW ? pos : line0 + line;
     V v = s[e];
     T m = T(1);
-    if (f.sign && ((i + j) & 1)) m = -m;
+    if (f.sign && ((f.sign == 1 ? i + j : (f.sign == 2 ? i : j)) & 1)) m = -m;
     if (mk) {
       T q = mk[(long long)i * ncols + j];
       m *= q;
@@ -131,6 +131,28 @@ __device__ __forceinline__ void store_tile(V* __restrict__ dst, const V* s, int 
   }
 }
 
+// deterministic per-block sum of |v|^2 over the tile (row passes)
+template <typename V, class Tile, int NT>
+__device__ __forceinline__ void row_abs2(const V* s, const AwPassArgs& a, int tid, int inst) {
+  constexpr int TILE = Tile::N * Tile::LINES;
+  constexpr int E = TILE / NT;
+  __shared__ double red2[NT];
+  double acc = 0.0;
+#pragma unroll 4
+  for (int k = 0; k < E; ++k) {
+    V v = s[tid + k * NT];
+    acc += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+  }
+  red2[tid] = acc;
+  __syncthreads();
+  for (int w = NT / 2; w > 0; w >>= 1) {
+    if (tid < w) red2[tid] += red2[tid + w];
+    __syncthreads();
+  }
+  if (tid == 0) a.red_abs2[(long long)inst * gridDim.x + blockIdx.x] = red2[0];
+  __syncthreads();
+}
+
 template <typename V, class Tile, int NT>
 __global__ void __launch_bounds__(NT) aw_pass_kernel(const AwPassArgs a) {
   extern __shared__ __align__(16) unsigned char aw_smem[];
@@ -167,22 +189,7 @@ __global__ void __launch_bounds__(NT) aw_pass_kernel(const AwPassArgs a) {
       }
     }
   }
-  if (Tile::IS_ROW && a.red_abs2) {
-    __shared__ double red2[NT];
-    double acc = 0.0;
-#pragma unroll 4
-    for (int k = 0; k < E; ++k) {
-      V v = s[tid + k * NT];
-      acc += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
-    }
-    red2[tid] = acc;
-    __syncthreads();
-    for (int w = NT / 2; w > 0; w >>= 1) {
-      if (tid < w) red2[tid] += red2[tid + w];
-      __syncthreads();
-    }
-    if (tid == 0) a.red_abs2[(long long)inst * gridDim.x + blockIdx.x] = red2[0];
-  }
+  if (Tile::IS_ROW && a.red_abs2 && !a.abs2_end) row_abs2<V, Tile, NT>(s, a, tid, inst);
   if (a.br_out) {
     V keep[E];
 #pragma unroll
@@ -200,6 +207,7 @@ __global__ void __launch_bounds__(NT) aw_pass_kernel(const AwPassArgs a) {
   run_fft<Tile, NT>(s, tw, a.d2, tid);
   if (a.f3.active) apply_factor<V, Tile, NT>(s, a.f3, line0, ncols, tid, toff, eoff, inst);
   if (a.out) store_tile<V, Tile, NT>((V*)a.out + eoff, s, line0, ncols, tid, false);
+  if (Tile::IS_ROW && a.red_abs2 && a.abs2_end) row_abs2<V, Tile, NT>(s, a, tid, inst);
 
   if (!Tile::IS_ROW && (a.red_line || a.red_cross || a.red_sq)) {
     // deterministic reductions over the column slab (fixed order, no atomics)
@@ -301,6 +309,16 @@ template <typename V> static int launch_col(const AwPassArgs* a, int batch, cuda
     case 2048: return launch_col_n<V, 2048>(a, batch, st);
     case 4096: return launch_col_n<V, 4096>(a, batch, st);
     case 8192: return launch_col_n<V, 8192>(a, batch, st);
+    default: return -1;
+  }
+}
+
+template <typename V> static int row_lines(int ncols) {
+  switch (ncols) {
+#define AW_RL(NN) \
+  case NN: return PassShape<V>::template Row<NN>::L;
+    AW_RL(64) AW_RL(128) AW_RL(256) AW_RL(512) AW_RL(1024) AW_RL(2048) AW_RL(4096) AW_RL(8192)
+#undef AW_RL
     default: return -1;
   }
 }

@@ -29,7 +29,7 @@ typedef struct AwFactor {
   const double* scale_ptr;  // optional device scalar: complex (re, im), one per instance
   double scale;
   int mask_pow;             // 0: no mask
-  int sign;                 // multiply by (-1)^(i+j)
+  int sign;                 // 1: multiply by (-1)^(i+j); 2: by (-1)^i; 3: by (-1)^j
   int sh_lo_n;              // 0: no shear
   int sh_roll;              // shear position index is (pos + sh_roll) mod npos
   int active;
@@ -56,7 +56,8 @@ typedef struct AwPassArgs {
   double* red_cross;        // column pass: [block][row], sum of Re over the block's columns
   double* red_sq;           // column pass: [block], sum of Re(v*v)
   double2* diag_out;        // row pass: element (i, i) at the branch point
-  double* red_abs2;         // row pass: [block], sum of |v|^2 at the branch point
+  double* red_abs2;         // row pass: [block], sum of |v|^2 at the branch point (or at the end)
+  int abs2_end;             // take red_abs2 after f3 instead of at the branch point
   const int* stop;          // when non-zero the pass is skipped
   long long batch_elems;    // batched launches: elements per instance (blockIdx.y)
   long long batch_tab;      // ... table entries per instance
@@ -70,6 +71,10 @@ int aw_launch_row_pass_f32(const AwPassArgs* a, int batch, void* stream);
 int aw_launch_col_pass_f32(const AwPassArgs* a, int batch, void* stream);
 // number of column blocks (rows of red_cross) the column pass uses for a given N
 int aw_col_pass_blocks(int nrows, int ncols, int f32);
+// number of rows one row-pass block holds for a row length ncols
+int aw_row_pass_lines(int ncols, int f32);
+// number of blocks of a row pass over nrows rows
+int aw_row_pass_blocks(int nrows, int ncols, int f32);
 
 #ifdef __cplusplus
 }

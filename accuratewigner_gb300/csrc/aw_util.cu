@@ -141,6 +141,68 @@ __global__ void k_trace_finalize(const double2* diag, int n, const double* abs2p
   }
 }
 
+// 1 / sqrt(Sum parts * scale): renormalisation of a wave function
+// (schrodinger_wigner_cuda_1d.py:388: psi /= norm(psi) * sqrt(dX))
+__global__ void k_norm_finalize(const double* parts, int nparts, double scale, double* inv_out, double* hist) {
+  __shared__ double r[256];
+  const int t = threadIdx.x;
+  double s = 0.0;
+  for (int k = t; k < nparts; k += blockDim.x) s += parts[k];
+  r[t] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (t < w) r[t] += r[t + w];
+    __syncthreads();
+  }
+  if (t == 0) {
+    inv_out[0] = 1.0 / sqrt(r[0] * scale);
+    inv_out[1] = 0.0;
+    if (hist) hist[0] = r[0];
+  }
+}
+
+// |a|^2 as a real array
+__global__ void k_abs2(const void* a, int f32, long long n, double* out) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    double2 v = ld(a, k, f32);
+    out[k] = v.x * v.x + v.y * v.y;
+  }
+}
+
+// partial sums of conj(a) * b (the reference's vdot ReductionKernel, sw:524-530)
+__global__ void k_vdot(const void* a, const void* b, int f32, long long n, double2* part) {
+  __shared__ double rr[256], ri[256];
+  double sr = 0.0, si = 0.0;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const double2 x = ld(a, k, f32), y = ld(b, k, f32);
+    sr += x.x * y.x + x.y * y.y;
+    si += x.x * y.y - x.y * y.x;
+  }
+  const int t = threadIdx.x;
+  rr[t] = sr;
+  ri[t] = si;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (t < w) {
+      rr[t] += rr[t + w];
+      ri[t] += ri[t + w];
+    }
+    __syncthreads();
+  }
+  if (t == 0) part[blockIdx.x] = make_double2(rr[0], ri[0]);
+}
+
+// y += (cr + i ci) x  (the reference's projectout ElementwiseKernel with C = -proj, sw:532-535)
+__global__ void k_axpy(void* y, const void* x, int f32, long long n, double cr, double ci) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const double2 a = ld(x, k, f32);
+    double2 b = ld(y, k, f32);
+    b.x += cr * a.x - ci * a.y;
+    b.y += cr * a.y + ci * a.x;
+    st(y, k, f32, b);
+  }
+}
+
 __global__ void k_set2(double* p, double a, double b) {
   p[0] = a;
   p[1] = b;
@@ -187,6 +249,22 @@ int aw_k_trace_finalize(const double2* diag, int n, const double* abs2part, int 
                         double* inv_out, double* hist, int* stop, int stop_on_purity, void* s) {
   k_trace_finalize<<<1, 256, 0, (cudaStream_t)s>>>(diag, n, abs2part, nparts, dX, complex_trace, inv_out, hist, stop,
                                                    stop_on_purity);
+  return ok();
+}
+int aw_k_norm_finalize(const double* parts, int nparts, double scale, double* inv_out, double* hist, void* s) {
+  k_norm_finalize<<<1, 256, 0, (cudaStream_t)s>>>(parts, nparts, scale, inv_out, hist);
+  return ok();
+}
+int aw_k_abs2(const void* a, int f32, long long n, double* out, void* s) {
+  k_abs2<<<grid_for(n), 256, 0, (cudaStream_t)s>>>(a, f32, n, out);
+  return ok();
+}
+int aw_k_vdot(const void* a, const void* b, int f32, long long n, double2* part, int nblocks, void* s) {
+  k_vdot<<<nblocks, 256, 0, (cudaStream_t)s>>>(a, b, f32, n, part);
+  return ok();
+}
+int aw_k_axpy(void* y, const void* x, int f32, long long n, double cr, double ci, void* s) {
+  k_axpy<<<grid_for(n), 256, 0, (cudaStream_t)s>>>(y, x, f32, n, cr, ci);
   return ok();
 }
 int aw_k_set2(double* p, double a, double b, void* s) {

@@ -185,6 +185,7 @@ int aw_gibbs(aw_handle h, double dbeta, int64_t steps, int64_t* done, double* pu
  * Gram-Schmidt against the stored stationary states instead). */
 int aw_sw_imag_steps(aw_handle h, int64_t steps, int32_t project);
 int aw_sw_store_state(aw_handle h);                 /* append psi to the stationary states */
+int aw_sw_clear_states(aw_handle h);                /* forget the stored stationary states */
 int aw_sw_get_state(aw_handle h, int32_t index, void* dst_host);
 int aw_sw_energy(aw_handle h, double t, double* out); /* get_energy, sw:461-482 */
 

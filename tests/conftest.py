@@ -34,3 +34,19 @@ def rel_l2(a, b):
     a = np.asarray(a)
     b = np.asarray(b)
     return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+def obs_close(a, b, tol, scale=1.0):
+    """Observable histories agree to `tol` relative to max(|b|, scale).
+
+    Observables that pass through zero (a centred <x>) are compared against
+    their natural scale (order one in atomic units) instead of their own size.
+    """
+    import numpy as np
+
+    a = np.asarray(a, dtype=float)
+    b = np.asarray(b, dtype=float)
+    if a.shape != b.shape:
+        return False
+    ref = max(float(np.abs(b).max()) if b.size else 0.0, scale)
+    return float(np.abs(a - b).max()) <= tol * ref
