@@ -35,7 +35,7 @@ __device__ double E(double t)
 __device__ double cosmask(double x, double xmax)
 {
     const double a = fabs(x) - 0.9 * xmax;
-    return a > 0. ? pow(cos(0.5 * M_PI * a / (0.1 * xmax)), 0.125) : 1.;
+    return a > 0. ? pow(fabs(cos(0.5 * M_PI * fmin(a / (0.1 * xmax), 1.))), 0.125) : 1.;
 }
 """
 
@@ -47,8 +47,8 @@ def e_field(t, E0=0.04, omega=0.057, ncyc=5):
 
 def cosmask(x, xmax):
     a = np.abs(x) - 0.9 * xmax
-    with np.errstate(invalid="ignore"):
-        return np.where(a > 0, np.power(np.abs(np.cos(0.5 * np.pi * np.maximum(a, 0) / (0.1 * xmax))), 0.125), 1.0)
+    r = np.minimum(np.maximum(a, 0.0) / (0.1 * xmax), 1.0)
+    return np.where(a > 0, np.power(np.abs(np.cos(0.5 * np.pi * r)), 0.125), 1.0)
 
 
 N_GRID = 1024
