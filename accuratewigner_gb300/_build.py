@@ -17,7 +17,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libawigner.so")
 
-SOURCES = ["aw_api.cu", "aw_util.cu", "aw_pass_f64.cu", "aw_pass_f32.cu"]
+SOURCES = ["aw_api.cu", "aw_util.cu", "aw_pass_f64.cu", "aw_pass_f32.cu", "aw_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 

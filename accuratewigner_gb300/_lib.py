@@ -117,6 +117,7 @@ SIGNATURES = [
     ("aw_sw_clear_states", c_int, [c_vp]),
     ("aw_sw_get_state", c_int, [c_vp, c_int, c_vp]),
     ("aw_sw_energy", c_int, [c_vp, c_dbl, ctypes.POINTER(c_dbl)]),
+    ("aw_reduce_noalloc", c_int, [c_vp, c_int, c_i64, c_i64, c_int, c_vp, c_vp]),
 ]
 
 _lib = None

@@ -477,6 +477,9 @@ static int dsum(aw_state_s* h, const void* p, long long n, int mode, long long s
 static double* dscal(aw_state_s* h, int k) { return (double*)h->scal.p + k; }
 
 // ============================================================================ creation
+// error message setter for the other translation units of the library (C++ linkage, not exported API)
+void aw_internal_set_error(const char* msg) { g_err = msg ? msg : ""; }
+
 extern "C" int32_t aw_version(void) { return AW_VERSION; }
 extern "C" const char* aw_last_error(void) { return g_err.c_str(); }
 extern "C" int64_t aw_launch_count(void) { return g_launches.load(); }

@@ -189,6 +189,21 @@ int aw_sw_clear_states(aw_handle h);                /* forget the stored station
 int aw_sw_get_state(aw_handle h, int32_t index, void* dst_host);
 int aw_sw_energy(aw_handle h, double t, double* out); /* get_energy, sw:461-482 */
 
+/* Buffer reduction that allocates nothing (no counterpart in the reference).
+ * For callers that cannot allocate device memory: a host application that owns
+ * the whole device memory budget and hands the library only pointers into its
+ * own pool, or a latency-critical loop where cudaMalloc / cudaFree would
+ * synchronise the device.  Same sums as aw_sum (mode 0: Sum a, complex),
+ * aw_purity (mode 1: Sum Re(a*a)), |a|^2 (mode 2) and aw_trace (mode 3: Sum of
+ * a[k * stride], k < n), over n complex128 (elem_bytes 16) or complex64 (8)
+ * elements at `data`; writes out_device[0..1] = (re, im), stream-ordered on
+ * `stream`.  Scratch is a 16 KiB static device array: at most 67108864
+ * elements per call (larger n is rejected with AW_E_ARG).  The first call on a
+ * device looks up that array's address; make it before any stream capture.
+ * Calls overlapping on the GPU race on the shared array. */
+int aw_reduce_noalloc(const void* data, int32_t elem_bytes, int64_t n, int64_t stride, int32_t mode,
+                      double* out_device, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
