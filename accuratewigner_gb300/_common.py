@@ -153,6 +153,7 @@ class TermTable:
         cfg.term_index = idx
         cfg.term_coef = coef
         cfg.n_slots = self.n_slots
+        cfg.obs_p_time_dependent = int(any(self.info.depends_on(e, "t") for e in self.obs_p))
 
 
 def precision_code(kwargs):

@@ -77,6 +77,7 @@ class AwConfig(ctypes.Structure):
         ("term_index", ctypes.POINTER(c_int)),
         ("term_coef", ctypes.POINTER(c_dbl)),
         ("n_slots", c_int),
+        ("obs_p_time_dependent", c_int),
     ]
 
 

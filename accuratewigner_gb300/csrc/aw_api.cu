@@ -141,6 +141,7 @@ struct aw_state_s {
   cudaStream_t st = nullptr;
   cudaLibrary_t lib = nullptr;
   cudaKernel_t k_tab = nullptr, k_values = nullptr, k_final = nullptr, k_mask2d = nullptr;
+  cudaKernel_t k_final_rot = nullptr;
   std::unordered_map<std::string, cudaKernel_t> obs_kernels;
   // buffers
   DevBuf rho, W, snap, tmp, stage;
@@ -154,6 +155,9 @@ struct aw_state_s {
   DevBuf hist;
   DevBuf terms;                        // term tables for the finalize kernel
   DevBuf part;                         // reduction partials (double2 x 1024)
+  DevBuf zbuf, altbuf;                 // rotated-frame marginal inputs (z | w, per-block partials of w)
+  int z_lines = 0, z_blocks = 0;       // column pass of the marginals: columns per block, partial rows
+  int z_cluster = 1;                   // ... and blocks per cluster
   DevBuf blk_tabs;                     // Blackman tables
   int shx_lo_n = 0, shy_lo_n = 0;
   DevBuf twist_hi, twist_lo;           // von Neumann momentum-diagonal twist exp(2 pi i k i / N) / N
@@ -445,7 +449,7 @@ static int build_tab(aw_state_s* h, int slot, int fn, int mode, double ta, doubl
   void* args[] = {&col, &row, &f32, &fn, &mode, &ncol, &dcol, &roll, &nrow, &drow,
                   &ta, &tb, &ca, &cb, &shift, &maskpow, &tmask};
   const int n = ncol + nrow;
-  return hjit(h, h->k_tab, dim3((n + 255) / 256), dim3(256), args);
+  return hjit(h, h->k_tab, dim3((n + 31) / 32), dim3(32), args);
 }
 
 static int build_mask2d(aw_state_s* h, int which, double t) {
@@ -538,7 +542,10 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   TRY(jit_kernel(h->lib, "aw_tab", &h->k_tab));
   TRY(jit_kernel(h->lib, "aw_values", &h->k_values));
   TRY(jit_kernel(h->lib, "aw_finalize", &h->k_final));
-  if (h->kn.rotated) TRY(jit_kernel(h->lib, "aw_mask2d", &h->k_mask2d));
+  if (h->kn.rotated) {
+    TRY(jit_kernel(h->lib, "aw_mask2d", &h->k_mask2d));
+    TRY(jit_kernel(h->lib, "aw_finalize_rot", &h->k_final_rot));
+  }
 
   // buffers
   const size_t grid = (size_t)(h->kn.sw ? h->sw_rows : h->nr) * h->nc;
@@ -549,10 +556,10 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   CK(cudaMemset(h->rho.p, 0, grid * h->esz));
   CK(cudaMemset(h->W.p, 0, wgrid * h->esz));
   TRY(dalloc(h->tabs, (size_t)TAB_NSLOT * (h->nc + h->nr) * h->esz));
-  TRY(dalloc(h->scal, 64 * sizeof(double)));
+  TRY(dalloc(h->scal, 2048 * sizeof(double)));
   TRY(dalloc(h->stop, 16 * sizeof(int)));
   TRY(dalloc(h->part, 1024 * sizeof(double2)));
-  CK(cudaMemset(h->scal.p, 0, 64 * sizeof(double)));
+  CK(cudaMemset(h->scal.p, 0, 2048 * sizeof(double)));
   CK(cudaMemset(h->stop.p, 0, 16 * sizeof(int)));
   {
     // term tables: int slot[64], kind[64], idx[64], double coef[64]
@@ -615,6 +622,16 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   TRY(dalloc(h->rowsum, (size_t)std::max(wr, wc) * 8));
   TRY(dalloc(h->diag, (size_t)std::max(h->nr, h->nc) * 16));
   TRY(dalloc(h->abs2, (size_t)std::max(h->nr, 1) * 8));
+  if (h->kn.rotated) {
+    // the marginal column pass: narrow slabs spread over every SM, row partials summed across
+    // clusters of 8 blocks in distributed shared memory, so that z_blocks stays small
+    h->z_lines = std::min(2, aw_col_pass_max_lines(h->nr, h->nc, h->f32));
+    const size_t z_smem = (size_t)h->nr * h->z_lines * h->esz + (size_t)h->nr * 16;
+    h->z_cluster = (h->nc / h->z_lines) % 8 == 0 && h->nr % 8 == 0 && z_smem <= 160 * 1024 ? 8 : 1;
+    h->z_blocks = h->nc / h->z_lines / h->z_cluster;
+    TRY(dalloc(h->zbuf, (size_t)(h->nc + h->nr) * 16));
+    TRY(dalloc(h->altbuf, (size_t)h->z_blocks * h->nr * 16));
+  }
 
   // 2-D absorbing masks of the rotated frame
   if (h->kn.rotated) {
@@ -682,7 +699,7 @@ extern "C" int aw_create(const aw_config* cfg, aw_handle* out) {
 extern "C" int aw_destroy(aw_handle h) {
   if (!h) return AW_OK;
   if (h->st) cudaStreamSynchronize(h->st);
-  DevBuf* bufs[] = {&h->twist_hi, &h->twist_lo, &h->rho, &h->W, &h->snap, &h->tmp, &h->stage, &h->tw_r, &h->tw_c, &h->tw_w, &h->shx_hi,
+  DevBuf* bufs[] = {&h->zbuf, &h->altbuf, &h->twist_hi, &h->twist_lo, &h->rho, &h->W, &h->snap, &h->tmp, &h->stage, &h->tw_r, &h->tw_c, &h->tw_w, &h->shx_hi,
                     &h->shx_lo, &h->shy_hi, &h->shy_lo, &h->tabs, &h->maskx, &h->maskp, &h->red_line,
                     &h->red_cross, &h->red_sq, &h->rowsum, &h->diag, &h->abs2, &h->scal, &h->stop, &h->hist,
                     &h->terms, &h->part, &h->blk_tabs};
@@ -1037,6 +1054,31 @@ static int launch_finalize(aw_state_s* h, double t, double* hist_row, int stop_o
   return launch_finalize_args(h, f, t, hist_row, stop_on_purity);
 }
 
+static int launch_finalize_rot(aw_state_s* h, double t, double* hist_row, int stop_on_purity) {
+  const double2* z = (const double2*)h->zbuf.p;
+  const double2* wpart = (const double2*)h->altbuf.p;
+  int nparts = h->z_blocks;
+  const double* abs2 = (const double*)h->abs2.p;
+  int nb2 = aw_row_pass_blocks(h->nr, h->nc, h->f32);
+  double* tv = dscal(h, 16);
+  unsigned int* counter = (unsigned int*)h->stop.p + 1;
+  double* inv = dscal(h, 0);
+  int* stop = (int*)h->stop.p;
+  int ncol = h->nc, nrow = h->nr;
+  double dX = h->cfg.dX, dP = h->cfg.dP, dXdP = h->cfg.dXdP;
+  const int* ts = (const int*)h->terms.p;
+  const int* tk = ts + 64;
+  const int* ti = ts + 128;
+  const double* tc = (const double*)((const char*)h->terms.p + 64 * 3 * sizeof(int));
+  int nterms = (int)h->tslot.size(), nslots = h->cfg.n_slots;
+  // chunks per term: enough blocks to spread the FP64 expression work over the SMs
+  int nchunk = 16;
+  while (nchunk > 1 && ((std::min(ncol, nrow) % nchunk) || (nterms + 2) * nchunk > 1024)) nchunk >>= 1;
+  void* args[] = {&z, &wpart, &nparts, &abs2, &nb2, &tv, &counter, &hist_row, &inv, &stop, &stop_on_purity, &t,
+                  &ncol, &nrow, &dX, &dP, &dXdP, &ts, &tk, &ti, &tc, &nterms, &nslots, &nchunk};
+  return hjit(h, h->k_final_rot, dim3((nterms + 2) * nchunk), dim3(128), args);
+}
+
 static int ensure_hist(aw_state_s* h, long long rows) {
   h->hist_cols = h->cfg.n_slots + 2;
   const size_t need = (size_t)std::max(rows, 1LL) * h->hist_cols * 8;
@@ -1159,15 +1201,22 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
   if (p.stop_on_purity) CK(cudaMemsetAsync(h->stop.p, 0, sizeof(int), h->st));
   const int* stop = p.stop_on_purity ? (const int*)h->stop.p : nullptr;
 
-  if (!vdep) TRY(rot_tables_V(h, p, times[1], times[1], true));
+  if (!vdep) TRY(rot_tables_V(h, p, times[1], times[1], false));
   if (!kdep) TRY(rot_tables_K(h, p, times[1]));
+  // with a time-dependent V the kick tables alternate between two slots, so that each time
+  // point's table is built once: slot of step n holds exp(-i dt/2 V(., t_n + dt/2))
+  auto vslot = [&](long long n) { return (!vdep || (n & 1)) ? TAB_V1 : TAB_V1B; };
+  auto vbuild = [&](long long n) -> int {
+    const double half = 0.5 * c.dt;
+    return build_tab(h, vslot(n), 0, 0, times[n] + half, 0.0, -half, 0.0, 0.0, 0, 0.0);
+  };
 
   // first kick: rho (position) -> S V(t_1) -> fft1
   {
-    if (vdep) TRY(rot_tables_V(h, p, times[1], 0.0, false));
+    if (vdep) TRY(vbuild(1));
     AwPassArgs a = pnone(h);
     a.in = a.out = h->rho.p;
-    TRY(vkick(h, p, TAB_V1, true, times[1], &a.f2));
+    TRY(vkick(h, p, vslot(1), true, times[1], &a.f2));
     a.d2 = +1;
     a.stop = stop;
     TRY(row_pass(h, a, h->tw_r));
@@ -1199,23 +1248,24 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
     }
     // row pass: ifft1, V-kick(t_n) [branch: Wigner transform] [next kick(t_{n+1}), fft1 | S]
     {
-      if (vdep) TRY(rot_tables_V(h, p, times[n], last ? 0.0 : times[n + 1], !last));
+      if (vdep && !last) TRY(vbuild(n + 1));
       AwPassArgs a = pnone(h);
       a.in = a.out = h->rho.p;
       a.d1 = -1;
-      TRY(vkick(h, p, TAB_V1, false, times[n], &a.f1));
+      TRY(vkick(h, p, vslot(n), false, times[n], &a.f1));
       if (p.ehrenfest) {
         a.br_out = h->W.p;
         a.br_d1 = +1;
         a.fbr = fshear_x(h);
         a.br_d2 = -1;
+        a.red_abs2 = (double*)h->abs2.p;  // Sum |rho_n|^2 for the purity
       }
       if (p.keep_rho) {
         a.mid_out = h->snap.p;
         a.mid_sign = 1;
       }
       if (!last) {
-        TRY(vkick(h, p, p.bloch ? TAB_BV : (vdep ? TAB_V1B : TAB_V1), false, times[n + 1], &a.f2));
+        TRY(vkick(h, p, vslot(n + 1), false, times[n + 1], &a.f2));
         a.d2 = +1;
       } else {
         a.f2 = fsign();
@@ -1224,32 +1274,25 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       TRY(row_pass(h, a, h->tw_r));
     }
     if (p.ehrenfest) {
-      // column / row / column passes of the transform; the last one reduces
+      // The per-step observables need only the marginals of W = S ifft0 C ifft0 (shY . fft0 A), where
+      // A is the branch output and C the second X shear; both marginals follow from Q_j = shY . fft0 A_j
+      // by alternating sums (aw_finalize_rot), so this column pass runs one FFT per column and writes
+      // nothing back.  The last step completes W.
       AwPassArgs a = pnone(h);
-      a.in = a.out = h->W.p;
+      a.in = h->W.p;
       a.d1 = +1;
       a.f1 = fshear_y(h);
-      a.d2 = -1;
+      a.col_alt = (double2*)h->zbuf.p;
+      a.alt_cross = (double2*)h->altbuf.p;
+      a.lines_hint = h->z_lines;
+      a.cluster = h->z_cluster;
       a.stop = stop;
       TRY(col_pass(h, a, h->tw_c));
-      a = pnone(h);
-      a.in = a.out = h->W.p;
-      a.d1 = +1;
-      a.f1 = fshear_x(h);
-      a.d2 = -1;
-      a.stop = stop;
-      TRY(row_pass(h, a, h->tw_r));
-      a = pnone(h);
-      a.in = h->W.p;
-      a.out = (last || p.stop_on_purity) ? h->W.p : nullptr;
-      a.d1 = -1;
-      a.f3 = fsign();
-      a.red_line = (double*)h->red_line.p;
-      a.red_cross = (double*)h->red_cross.p;
-      a.red_sq = (double*)h->red_sq.p;
-      a.stop = stop;
-      TRY(col_pass(h, a, h->tw_c));
-      TRY(launch_finalize(h, times[n], hist + (size_t)(n - 1) * h->hist_cols, p.stop_on_purity));
+      TRY(launch_finalize_rot(h, times[n], hist + (size_t)(n - 1) * h->hist_cols, p.stop_on_purity));
+      if (last) {
+        WignerGrid g{h->W.p, h->nr, h->nc, &h->tw_r, &h->tw_c};
+        TRY(wigner_passes(h, g, h->W.p, fnone(), false, false, true, true));
+      }
     }
   }
   return AW_OK;
@@ -1403,6 +1446,10 @@ extern "C" int aw_gibbs(aw_handle h, double dbeta, int64_t steps, int64_t* done,
   if (purity && ran > 0) *purity = hh[(size_t)(ran - 1) * cols + cols - 2];
   // rho_n of the last executed step (position representation, unnormalised) and its W
   CK(cudaMemcpyAsync(h->rho.p, h->snap.p, (size_t)h->nr * h->nc * h->esz, cudaMemcpyDeviceToDevice, h->st));
+  {
+    WignerGrid g{h->W.p, h->nr, h->nc, &h->tw_r, &h->tw_c};
+    TRY(wigner_passes(h, g, h->rho.p, fsign(), false, false, true));
+  }
   KL(aw_k_scale(h->W.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
   KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
   CK(cudaStreamSynchronize(h->st));

@@ -1,4 +1,4 @@
-// Shared-memory Stockham FFT over a tile of independent lines.
+// Stockham FFT over a tile of independent lines, registers + shared memory.
 //
 // Replaces the reference's batched cuFFT Z2Z plans (cufft.py:274-343): a
 // row-pass tile holds whole rows (the Axis1 plan), a column-pass tile holds
@@ -7,48 +7,47 @@
 //
 // Algorithm: the radix-R Stockham autosort FFT (Govindaraju et al., SC08,
 // "High Performance Discrete Fourier Transforms on Graphics Processors"),
-// mixed radix 8/4/2, in place in shared memory: every stage reads all of its
-// inputs into registers, synchronises, then writes its outputs.  Twiddles
-// come from a per-N table tw[m] = exp(-2 pi i m / N) built on the host in
-// extended precision and rounded once.
+// mixed radix 8/4/2.  Twiddles come from a per-N table
+// tw[m] = exp(-2 pi i m / N) built on the host in extended precision.
+//
+// Data placement.  Each thread owns E elements of the tile, all on one line:
+//   line = tid % LINES,  position p_k = tid / LINES + k * (N / E),  k = 0..E-1.
+// The first Stockham stage (span 1) of radix 8 reads exactly these elements
+// and the last stage writes exactly these positions, so an FFT starts from
+// and ends in registers; only the stages in between go through shared memory
+// (read all inputs, synchronise, write all outputs).  Element-wise factors,
+// global loads and stores and reductions all work on the registers.
 #pragma once
 #include "aw_common.cuh"
 
-// Tile geometry: a row tile holds L lines of N contiguous elements; a column
-// tile holds B lines interleaved (element e of line c sits at e*B + c), which
-// is exactly the layout of a B-column slab of a row-major grid.
+// Tile geometry: a row tile holds L lines of N contiguous elements (padded by
+// one element per line when L > 1 so that lanes on different lines fall in
+// different banks); a column tile holds B lines interleaved (element e of line
+// c sits at e*B + c), the layout of a B-column slab of a row-major grid.
+// In both, consecutive work items walk across lines first.
 template <int N_, int L_> struct RowTile {
   static constexpr int N = N_;
   static constexpr int LINES = L_;
   static constexpr bool IS_ROW = true;
-  __device__ __forceinline__ static int addr(int line, int e) { return line * N + e; }
-  // consecutive work items walk along a line
-  __device__ __forceinline__ static void split(int u, int nb, int& line, int& b) {
-    line = u / nb;
-    b = u - line * nb;
-  }
-  // element index in the tile -> (line, position)
-  __device__ __forceinline__ static void elem(int e, int& line, int& pos) {
-    line = e / N;
-    pos = e - line * N;
-  }
+  static constexpr int STRIDE = L_ > 1 ? N_ + 1 : N_;
+  static constexpr int SMEM_ELEMS = STRIDE * L_;
+  __device__ __forceinline__ static int addr(int line, int e) { return line * STRIDE + e; }
 };
 
 template <int N_, int B_> struct ColTile {
   static constexpr int N = N_;
   static constexpr int LINES = B_;
   static constexpr bool IS_ROW = false;
+  static constexpr int SMEM_ELEMS = N_ * B_;
   __device__ __forceinline__ static int addr(int line, int e) { return e * B_ + line; }
-  // consecutive work items walk across lines (neighbouring columns)
-  __device__ __forceinline__ static void split(int u, int nb, int& line, int& b) {
-    b = u / B_;
-    line = u - b * B_;
-  }
-  __device__ __forceinline__ static void elem(int e, int& line, int& pos) {
-    pos = e / B_;
-    line = e - pos * B_;
-  }
 };
+
+// work item u -> (line, butterfly index b): lines first
+template <class Tile>
+__device__ __forceinline__ void split_item(int u, int& line, int& b) {
+  line = u % Tile::LINES;
+  b = u / Tile::LINES;
+}
 
 // ---------------------------------------------------------------- radix kernels
 template <int R, bool FWD, typename V> struct Dft;
@@ -102,7 +101,8 @@ template <int REM> struct RadixChoice {
   static constexpr int R = REM >= 8 ? 8 : REM;
 };
 
-// One Stockham stage with span NS (product of the radices already applied).
+// Middle Stockham stage with span NS: shared memory to shared memory, in place
+// (all inputs are read before the barrier, all outputs written after it).
 template <class Tile, int NT, int NS, bool FWD, typename V>
 __device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __restrict__ tw, int tid) {
   constexpr int N = Tile::N;
@@ -115,7 +115,7 @@ __device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __res
 #pragma unroll
   for (int m = 0; m < PER; ++m) {
     int line, b;
-    Tile::split(tid + m * NT, NB, line, b);
+    split_item<Tile>(tid + m * NT, line, b);
 #pragma unroll
     for (int r = 0; r < R; ++r) v[m][r] = s[Tile::addr(line, b + r * NB)];
   }
@@ -123,14 +123,12 @@ __device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __res
 #pragma unroll
   for (int m = 0; m < PER; ++m) {
     int line, b;
-    Tile::split(tid + m * NT, NB, line, b);
+    split_item<Tile>(tid + m * NT, line, b);
     const int k = b & (NS - 1);
-    if (NS > 1) {
 #pragma unroll
-      for (int r = 1; r < R; ++r) {
-        V w = tw[r * k * (N / (NS * R))];
-        v[m][r] = FWD ? cmul(v[m][r], w) : cmulc(v[m][r], w);
-      }
+    for (int r = 1; r < R; ++r) {
+      V w = tw[r * k * (N / (NS * R))];
+      v[m][r] = FWD ? cmul(v[m][r], w) : cmulc(v[m][r], w);
     }
     Dft<R, FWD, V>::run(v[m]);
     const int base = (b / NS) * NS * R + k;
@@ -140,24 +138,76 @@ __device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __res
   __syncthreads();
 }
 
-template <class Tile, int NT, int NS, bool FWD, typename V> struct StockhamRun {
+template <class Tile, int NT, int NS, bool FWD, typename V> struct MiddleStages {
+  // applies stages NS, NS*R, ... up to but excluding the last one
   __device__ __forceinline__ static void run(V* s, const V* tw, int tid) {
-    stockham_stage<Tile, NT, NS, FWD, V>(s, tw, tid);
-    StockhamRun<Tile, NT, NS * RadixChoice<Tile::N / NS>::R, FWD, V>::run(s, tw, tid);
+    constexpr int R = RadixChoice<Tile::N / NS>::R;
+    if constexpr (NS * R < Tile::N) {
+      stockham_stage<Tile, NT, NS, FWD, V>(s, tw, tid);
+      MiddleStages<Tile, NT, NS * R, FWD, V>::run(s, tw, tid);
+    }
   }
 };
 
-// terminates when the span reaches N
-template <int N, int L, int NT, bool FWD, typename V> struct StockhamRun<RowTile<N, L>, NT, N, FWD, V> {
-  __device__ __forceinline__ static void run(V*, const V*, int) {}
+template <int N, int NS> struct LastSpan {
+  static constexpr int R = RadixChoice<N / NS>::R;
+  static constexpr int value = NS * R >= N ? NS : LastSpan<N, NS * R>::value;
 };
-template <int N, int B, int NT, bool FWD, typename V> struct StockhamRun<ColTile<N, B>, NT, N, FWD, V> {
-  __device__ __forceinline__ static void run(V*, const V*, int) {}
+template <int N> struct LastSpan<N, N> {
+  static constexpr int value = N;
 };
 
-// Full in-place FFT of every line of the tile.  Expects the tile to be
-// complete in shared memory (caller synchronised); returns synchronised.
+// Full FFT of every line of the tile, registers in and out.
+//   r[k] holds the thread's element at position tid / LINES + k * (N / E) of line tid % LINES.
 template <class Tile, int NT, bool FWD, typename V>
-__device__ __noinline__ void tile_fft(V* s, const V* tw, int tid) {
-  StockhamRun<Tile, NT, 1, FWD, V>::run(s, tw, tid);
+__device__ __forceinline__ void tile_fft_regs(V* r, V* __restrict__ s, const V* __restrict__ tw, int tid) {
+  constexpr int N = Tile::N;
+  constexpr int L = Tile::LINES;
+  constexpr int E = N * L / NT;
+  constexpr int R1 = RadixChoice<N>::R;
+  static_assert(R1 == 8 && E % 8 == 0, "the first stage must be radix 8 over the thread's own elements");
+  constexpr int PER1 = E / R1;
+  // the previous use of the tile may still be read by other threads
+  __syncthreads();
+  // stage 1 (span 1): inputs are the thread's own elements, no twiddles
+#pragma unroll
+  for (int m = 0; m < PER1; ++m) {
+    V v[R1];
+#pragma unroll
+    for (int q = 0; q < R1; ++q) v[q] = r[m + q * PER1];
+    Dft<R1, FWD, V>::run(v);
+    int line, b;
+    split_item<Tile>(tid + m * NT, line, b);
+#pragma unroll
+    for (int q = 0; q < R1; ++q) s[Tile::addr(line, b * R1 + q)] = v[q];
+  }
+  __syncthreads();
+  MiddleStages<Tile, NT, R1, FWD, V>::run(s, tw, tid);
+  // last stage: span NSL = N / RL; outputs land on the thread's own positions
+  constexpr int NSL = LastSpan<N, R1>::value;
+  constexpr int RL = N / NSL;
+  constexpr int NBL = N / RL;
+  constexpr int PERL = L * NBL / NT;
+  V v[PERL][RL];
+#pragma unroll
+  for (int m = 0; m < PERL; ++m) {
+    int line, b;
+    split_item<Tile>(tid + m * NT, line, b);
+#pragma unroll
+    for (int q = 0; q < RL; ++q) v[m][q] = s[Tile::addr(line, b + q * NBL)];
+  }
+#pragma unroll
+  for (int m = 0; m < PERL; ++m) {
+    int line, b;
+    split_item<Tile>(tid + m * NT, line, b);
+    // b < NSL here, so the twiddle exponent is q * b and the outputs go to b + q * NSL
+#pragma unroll
+    for (int q = 1; q < RL; ++q) {
+      V w = tw[q * b];
+      v[m][q] = FWD ? cmul(v[m][q], w) : cmulc(v[m][q], w);
+    }
+    Dft<RL, FWD, V>::run(v[m]);
+#pragma unroll
+    for (int q = 0; q < RL; ++q) r[m + q * PERL] = v[m][q];
+  }
 }

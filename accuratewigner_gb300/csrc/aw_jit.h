@@ -245,6 +245,88 @@ extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw
 )AWSRC";
   if (kn.rotated) {
     s += R"AWSRC(
+// Per-step observables of the rotated frame from one column FFT of the Wigner transform's first
+// stage A (W = S ifft0 C ifft0 (shY . fft0 A), C = the second X shear; see rot_run in aw_api.cu).
+// With Q_j = shY_j . fft0(A_j):
+//   X-marginal  c_j = Sum_i Re W_ij = (-1)^j Np Re z_j,            z_j = Sum_m (-1)^m Q_j(m)
+//   P-marginal  r_i = Sum_j Re W_ij = (-1)^i Np Re w_{(-i) mod Np},  w_m = Sum_j (-1)^j Q_j(m)
+//   purity      2 pi dXdP Sum Re W^2 / norm^2 = 2 pi dXdP Np Sum |rho|^2 / norm^2 (the transform is
+//               unitary up to the factor Np of the unnormalised ifft0)
+// One block per term, one for the norm, one for Sum |rho|^2; the last block to finish combines
+// them in a fixed order.
+extern "C" __global__ void aw_finalize_rot(const double2* aw_z, const double2* aw_wpart, int aw_nparts,
+                                           const double* aw_abs2, int aw_nb2, double* aw_tv, unsigned int* aw_counter,
+                                           double* aw_hist, double* aw_inv_norm, int* aw_stop, int aw_stop_on_purity,
+                                           double t, int aw_ncol, int aw_nrow, double aw_dX, double aw_dP,
+                                           double aw_dXdP, const int* aw_tslot, const int* aw_tkind,
+                                           const int* aw_tidx, const double* aw_tcoef, int aw_nterms, int aw_nslots,
+                                           int aw_nchunk) {
+  // blocks: (term or norm or purity) x chunk; FP64 expression evaluation spread over the GPU
+  __shared__ double aw_red[256];
+  __shared__ int aw_is_last;
+  if (aw_stop && *aw_stop) return;
+  const int aw_q = blockIdx.x / aw_nchunk;      // 0..nterms-1 terms, nterms norm, nterms+1 purity
+  const int aw_c = blockIdx.x - aw_q * aw_nchunk;
+  const int aw_t = threadIdx.x;
+  const int aw_nt = blockDim.x;
+  double aw_s = 0.0;
+  if (aw_q < aw_nterms) {
+    const int aw_idx = aw_tidx[aw_q];
+    if (aw_tkind[aw_q] == 0) {
+      const int aw_len = aw_ncol / aw_nchunk, aw_lo = aw_c * aw_len;
+      for (int aw_j = aw_lo + aw_t; aw_j < aw_lo + aw_len; aw_j += aw_nt) {
+        const double X = aw_dX * ((aw_size_t)aw_j - 0.5 * aw_ncol);
+        const double aw_cj = ((aw_j & 1) ? -1.0 : 1.0) * aw_nrow * aw_z[aw_j].x;
+        aw_s += aw_cj * aw_obs_x(aw_idx, X, t);
+      }
+    } else {
+      const int aw_len = aw_nrow / aw_nchunk, aw_lo = aw_c * aw_len;
+      for (int aw_i = aw_lo + aw_t; aw_i < aw_lo + aw_len; aw_i += aw_nt) {
+        const double P = aw_dP * ((aw_size_t)aw_i - 0.5 * aw_nrow);
+        const int aw_k = (aw_nrow - aw_i) & (aw_nrow - 1);
+        double aw_w = 0.0;
+        for (int aw_p = 0; aw_p < aw_nparts; ++aw_p) aw_w += aw_wpart[(long long)aw_p * aw_nrow + aw_k].x;
+        aw_s += ((aw_i & 1) ? -1.0 : 1.0) * aw_nrow * aw_w * aw_obs_p(aw_idx, P, t);
+      }
+    }
+  } else if (aw_q == aw_nterms) {
+    const int aw_len = aw_ncol / aw_nchunk, aw_lo = aw_c * aw_len;
+    for (int aw_j = aw_lo + aw_t; aw_j < aw_lo + aw_len; aw_j += aw_nt)
+      aw_s += ((aw_j & 1) ? -1.0 : 1.0) * aw_nrow * aw_z[aw_j].x;
+  } else if (aw_abs2) {
+    for (int aw_p = aw_c * aw_nt + aw_t; aw_p < aw_nb2; aw_p += aw_nt * aw_nchunk) aw_s += aw_abs2[aw_p];
+  }
+  const double aw_v = aw_block_sum(aw_s, aw_red);
+  if (aw_t == 0) {
+    aw_tv[blockIdx.x] = aw_v;
+    __threadfence();
+    const unsigned int aw_prev = atomicAdd(aw_counter, 1u);
+    aw_is_last = aw_prev == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (aw_is_last && aw_t == 0) {
+    __threadfence();
+    const volatile double* aw_vt = aw_tv;
+    double aw_sum[66];
+    for (int aw_k = 0; aw_k < aw_nterms + 2; ++aw_k) {
+      double aw_acc = 0.0;
+      for (int aw_cc = 0; aw_cc < aw_nchunk; ++aw_cc) aw_acc += aw_vt[aw_k * aw_nchunk + aw_cc];
+      aw_sum[aw_k] = aw_acc;
+    }
+    const double aw_norm = aw_sum[aw_nterms] * aw_dXdP;
+    for (int aw_k = 0; aw_k < aw_nslots; ++aw_k) aw_hist[aw_k] = 0.0;
+    for (int aw_k = 0; aw_k < aw_nterms; ++aw_k)
+      aw_hist[aw_tslot[aw_k]] += aw_tcoef[aw_k] * (aw_sum[aw_k] * aw_dXdP / aw_norm);
+    const double aw_purity = 2.0 * M_PI * aw_dXdP * aw_nrow * aw_sum[aw_nterms + 1] / (aw_norm * aw_norm);
+    aw_hist[aw_nslots] = aw_purity;
+    aw_hist[aw_nslots + 1] = aw_norm;
+    aw_inv_norm[0] = 1.0 / aw_norm;
+    aw_inv_norm[1] = 0.0;
+    if (aw_stop && aw_stop_on_purity && !(aw_purity < 1.0)) *aw_stop = 1;
+    *aw_counter = 0u;
+  }
+}
+
 // 2-D absorbing boundaries of the rotated frame (expV / expK of
 // wigner_moyal_cuda_1d.py:742-778 multiply by these expressions).
 extern "C" __global__ void aw_mask2d(void* aw_out, int aw_f32, int aw_which, double t, int aw_nrow, int aw_ncol,

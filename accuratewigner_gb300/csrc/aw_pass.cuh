@@ -6,54 +6,50 @@
 // tile from HBM once, keeps it in shared memory for every FFT, phase multiply
 // and reduction of its program, and writes it once.
 #pragma once
+#include <cooperative_groups.h>
+
 #include "aw_common.cuh"
 #include "aw_fft.cuh"
 #include "aw_pass.h"
 
-template <typename V> struct PassShape;
+namespace cg = cooperative_groups;
 
-// complex128: 32 KB row tiles, 128 KB column slabs, 8 elements per thread
-template <> struct PassShape<double2> {
-  template <int N> struct Row {
-    static constexpr int L = N >= 2048 ? 1 : 2048 / N;
-    static constexpr int TILE = L * N;
-    static constexpr int E = TILE / 1024 > 8 ? TILE / 1024 : 8;
-    static constexpr int NT = TILE / E;
-  };
-  template <int N> struct Col {
-    static constexpr int B = N <= 1024 ? 8 : (8192 / N);
-    static constexpr int TILE = B * N;
-    static constexpr int E = TILE / 1024 > 8 ? TILE / 1024 : 8;
-    static constexpr int NT = TILE / E;
-  };
-};
-
-// complex64: 32 KB row tiles, 128 KB column slabs
-template <> struct PassShape<float2> {
-  template <int N> struct Row {
-    static constexpr int L = N >= 4096 ? 1 : 4096 / N;
-    static constexpr int TILE = L * N;
-    static constexpr int E = TILE / 1024 > 8 ? TILE / 1024 : 8;
-    static constexpr int NT = TILE / E;
-  };
-  template <int N> struct Col {
-    static constexpr int B = N <= 1024 ? 16 : (16384 / N);
-    static constexpr int TILE = B * N;
-    static constexpr int E = TILE / 1024 > 8 ? TILE / 1024 : 8;
-    static constexpr int NT = TILE / E;
-  };
+// Tile shapes.  A row tile holds LINES whole rows, a column tile a slab of
+// LINES whole columns; a thread keeps E elements (8, more for lines longer
+// than 8192 elements so that a block stays at or below 1024 threads).  The
+// number of lines per tile is chosen at run time (aw_row_pass_lines /
+// aw_col_pass_lines) so that a launch spreads over all 152 SMs.
+template <typename V, int N, int LINES> struct Shape {
+  static constexpr int TILE = N * LINES;
+  static constexpr int E = TILE / 1024 > 8 ? TILE / 1024 : 8;
+  static constexpr int NT = TILE / E;
+  static constexpr int SMEM_ELEMS = LINES > 1 ? (N + 1) * LINES : N;  // upper bound over both tile kinds
+  static constexpr bool FITS = (N + 1) * LINES * (int)sizeof(V) <= 128 * 1024;
 };
 
 template <typename V> struct RealOf;
 template <> struct RealOf<double2> { typedef double type; };
 template <> struct RealOf<float2> { typedef float type; };
 
-// apply one AwFactor to the thread's own elements of the tile
+// The thread's own elements (see aw_fft.cuh): line tid % LINES, positions pos0 + k * STEP.
+template <class Tile, int NT> struct Own {
+  static constexpr int E = Tile::N * Tile::LINES / NT;
+  static constexpr int STEP = Tile::N / E;
+};
+
+// global index of the element at (global line lg, position pos)
+template <class Tile>
+__device__ __forceinline__ long long gidx(int lg, int pos, int ncols) {
+  return Tile::IS_ROW ? (long long)lg * ncols + pos : (long long)pos * ncols + lg;
+}
+
+// apply one AwFactor to the thread's own elements
 template <typename V, class Tile, int NT>
-__device__ __forceinline__ void apply_factor(V* s, const AwFactor& f, int line0, int ncols, int tid,
+__device__ __forceinline__ void apply_factor(V* r, const AwFactor& f, int lg, int pos0, int ncols,
                                              long long tab_off, long long elem_off, int inst) {
   typedef typename RealOf<V>::type T;
-  constexpr int TILE = Tile::N * Tile::LINES;
+  constexpr int E = Own<Tile, NT>::E;
+  constexpr int STEP = Own<Tile, NT>::STEP;
   const V* ct = (const V*)f.col_tab;
   const V* rt = (const V*)f.row_tab;
   const T* mk = (const T*)f.mask;
@@ -68,14 +64,25 @@ __device__ __forceinline__ void apply_factor(V* s, const AwFactor& f, int line0,
     sc = (T)(f.scale * f.scale_ptr[2 * inst]);
     sci = (T)(f.scale * f.scale_ptr[2 * inst + 1]);
   }
-  const int nhi = f.sh_lo_n ? Tile::N / f.sh_lo_n : 0;
-#pragma unroll 4
-  for (int e = tid; e < TILE; e += NT) {
-    int line, pos;
-    Tile::elem(e, line, pos);
-    const int i = Tile::IS_ROW ? line0 + line : pos;
-    const int j = Tile::IS_ROW ? pos : line0 + line;
-    V v = s[e];
+  const int lo_n = f.sh_lo_n;
+  const int nhi = lo_n ? Tile::N / lo_n : 0;
+  // factors that depend only on the line
+  V line_w = cmake<V>(T(1), T(0));
+  bool have_line_w = false;
+  if (Tile::IS_ROW && rt) {
+    line_w = rt[lg];
+    have_line_w = true;
+  }
+  if (!Tile::IS_ROW && ct) {
+    line_w = ct[lg];
+    have_line_w = true;
+  }
+#pragma unroll
+  for (int k = 0; k < E; ++k) {
+    const int pos = pos0 + k * STEP;
+    const int i = Tile::IS_ROW ? lg : pos;
+    const int j = Tile::IS_ROW ? pos : lg;
+    V v = r[k];
     T m = T(1);
     if (f.sign && ((f.sign == 1 ? i + j : (f.sign == 2 ? i : j)) & 1)) m = -m;
     if (mk) {
@@ -84,251 +91,355 @@ __device__ __forceinline__ void apply_factor(V* s, const AwFactor& f, int line0,
       if (f.mask_pow == 2) m *= q;
     }
     v = sci == T(0) ? cscale(v, m * sc) : cmul(v, cmake<V>(m * sc, m * sci));
-    if (ct) v = cmul(v, ct[j]);
-    if (rt) v = cmulc(v, rt[i]);
-    if (f.sh_lo_n) {
-      const int lg = line0 + line;
+    if (Tile::IS_ROW) {
+      if (ct) v = cmul(v, ct[j]);
+      if (have_line_w) v = cmulc(v, line_w);
+    } else {
+      if (have_line_w) v = cmul(v, line_w);
+      if (rt) v = cmulc(v, rt[i]);
+    }
+    if (lo_n) {
       const int q = (pos + f.sh_roll) & (Tile::N - 1);
-      V w = cmul(sh[(long long)lg * nhi + q / f.sh_lo_n], sl[(long long)lg * f.sh_lo_n + (q % f.sh_lo_n)]);
+      V w = cmul(sh[(long long)lg * nhi + q / lo_n], sl[(long long)lg * lo_n + (q % lo_n)]);
       v = cmul(v, w);
     }
-    s[e] = v;
+    r[k] = v;
   }
 }
 
 template <class Tile, int NT, typename V>
-__device__ __forceinline__ void run_fft(V* s, const V* tw, int dir, int tid) {
+__device__ __forceinline__ void run_fft(V* r, V* s, const V* tw, int dir, int tid) {
   if (dir == 0) return;
-  __syncthreads();
   if (dir > 0)
-    tile_fft<Tile, NT, true, V>(s, tw, tid);
+    tile_fft_regs<Tile, NT, true, V>(r, s, tw, tid);
   else
-    tile_fft<Tile, NT, false, V>(s, tw, tid);
-}
-
-// global element offset of tile element e
-template <class Tile>
-__device__ __forceinline__ long long gofs(int e, int line0, int ncols) {
-  int line, pos;
-  Tile::elem(e, line, pos);
-  return Tile::IS_ROW ? (long long)(line0 + line) * ncols + pos : (long long)pos * ncols + line0 + line;
+    tile_fft_regs<Tile, NT, false, V>(r, s, tw, tid);
 }
 
 template <typename V, class Tile, int NT>
-__device__ __forceinline__ void store_tile(V* __restrict__ dst, const V* s, int line0, int ncols, int tid, bool sgn) {
-  constexpr int TILE = Tile::N * Tile::LINES;
-#pragma unroll 4
-  for (int e = tid; e < TILE; e += NT) {
-    V v = s[e];
-    if (sgn) {
-      int line, pos;
-      Tile::elem(e, line, pos);
-      const int i = Tile::IS_ROW ? line0 + line : pos;
-      const int j = Tile::IS_ROW ? pos : line0 + line;
-      if ((i + j) & 1) v = cmake<V>(-v.x, -v.y);
-    }
-    dst[gofs<Tile>(e, line0, ncols)] = v;
-  }
-}
-
-// deterministic per-block sum of |v|^2 over the tile (row passes)
-template <typename V, class Tile, int NT>
-__device__ __forceinline__ void row_abs2(const V* s, const AwPassArgs& a, int tid, int inst) {
-  constexpr int TILE = Tile::N * Tile::LINES;
-  constexpr int E = TILE / NT;
-  __shared__ double red2[NT];
-  double acc = 0.0;
-#pragma unroll 4
+__device__ __forceinline__ void store_regs(V* __restrict__ dst, const V* r, int lg, int pos0, int ncols, bool sgn) {
+  constexpr int E = Own<Tile, NT>::E;
+  constexpr int STEP = Own<Tile, NT>::STEP;
+#pragma unroll
   for (int k = 0; k < E; ++k) {
-    V v = s[tid + k * NT];
-    acc += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+    const int pos = pos0 + k * STEP;
+    V v = r[k];
+    if (sgn && ((lg + pos) & 1)) v = cmake<V>(-v.x, -v.y);
+    dst[gidx<Tile>(lg, pos, ncols)] = v;
   }
-  red2[tid] = acc;
+}
+
+// deterministic block sum of one double per thread (NT a power of two); result valid in thread 0
+template <int NT>
+__device__ __forceinline__ double block_sum(double x, double* red, int tid) {
+  red[tid] = x;
   __syncthreads();
+#pragma unroll 1
   for (int w = NT / 2; w > 0; w >>= 1) {
-    if (tid < w) red2[tid] += red2[tid + w];
+    if (tid < w) red[tid] += red[tid + w];
     __syncthreads();
   }
-  if (tid == 0) a.red_abs2[(long long)inst * gridDim.x + blockIdx.x] = red2[0];
+  const double out = red[0];
   __syncthreads();
+  return out;
 }
 
 template <typename V, class Tile, int NT>
 __global__ void __launch_bounds__(NT) aw_pass_kernel(const AwPassArgs a) {
   extern __shared__ __align__(16) unsigned char aw_smem[];
+  typedef typename RealOf<V>::type T;
   V* s = reinterpret_cast<V*>(aw_smem);
-  constexpr int TILE = Tile::N * Tile::LINES;
-  constexpr int E = TILE / NT;
+  constexpr int L = Tile::LINES;
+  constexpr int E = Own<Tile, NT>::E;
+  constexpr int STEP = Own<Tile, NT>::STEP;
+  __shared__ double red[NT];
   const int inst = blockIdx.y;
   if (a.stop && a.stop[inst]) return;
   const int tid = threadIdx.x;
-  const int line0 = blockIdx.x * Tile::LINES;
+  const int line = tid % L;
+  const int pos0 = tid / L;
+  const int line0 = blockIdx.x * L;
+  const int lg = line0 + line;
   const int ncols = a.ncols;
   const long long eoff = (long long)inst * a.batch_elems;
   const long long toff = (long long)inst * a.batch_tab;
   const V* in = (const V*)a.in + eoff;
   const V* tw = (const V*)a.tw;
 
-#pragma unroll 4
-  for (int e = tid; e < TILE; e += NT) s[e] = in[gofs<Tile>(e, line0, ncols)];
+  V r[E];
+#pragma unroll
+  for (int k = 0; k < E; ++k) r[k] = in[gidx<Tile>(lg, pos0 + k * STEP, ncols)];
 
-  if (a.f0.active) apply_factor<V, Tile, NT>(s, a.f0, line0, ncols, tid, toff, eoff, inst);
-  run_fft<Tile, NT>(s, tw, a.d1, tid);
-  if (a.f1.active) apply_factor<V, Tile, NT>(s, a.f1, line0, ncols, tid, toff, eoff, inst);
+  if (a.f0.active) apply_factor<V, Tile, NT>(r, a.f0, lg, pos0, ncols, toff, eoff, inst);
+  run_fft<Tile, NT>(r, s, tw, a.d1, tid);
+  if (a.f1.active) apply_factor<V, Tile, NT>(r, a.f1, lg, pos0, ncols, toff, eoff, inst);
 
-  if (a.mid_out) store_tile<V, Tile, NT>((V*)a.mid_out + eoff, s, line0, ncols, tid, a.mid_sign != 0);
+  if (a.mid_out) store_regs<V, Tile, NT>((V*)a.mid_out + eoff, r, lg, pos0, ncols, a.mid_sign != 0);
   if (Tile::IS_ROW && a.diag_out) {
-    // element (i, i) of each row at the branch point
-#pragma unroll 4
-    for (int e = tid; e < TILE; e += NT) {
-      int line, pos;
-      Tile::elem(e, line, pos);
-      if (line0 + line == pos) {
-        V v = s[e];
-        a.diag_out[(long long)inst * a.nrows + pos] = make_double2((double)v.x, (double)v.y);
-      }
-    }
+#pragma unroll
+    for (int k = 0; k < E; ++k)
+      if (pos0 + k * STEP == lg)
+        a.diag_out[(long long)inst * a.nrows + lg] = make_double2((double)r[k].x, (double)r[k].y);
   }
-  if (Tile::IS_ROW && a.red_abs2 && !a.abs2_end) row_abs2<V, Tile, NT>(s, a, tid, inst);
+  if (Tile::IS_ROW && a.red_abs2 && !a.abs2_end) {
+    T acc = T(0);
+#pragma unroll
+    for (int k = 0; k < E; ++k) acc += r[k].x * r[k].x + r[k].y * r[k].y;
+    const double tot = block_sum<NT>((double)acc, red, tid);
+    if (tid == 0) a.red_abs2[(long long)inst * gridDim.x + blockIdx.x] = tot;
+  }
   if (a.br_out) {
     V keep[E];
 #pragma unroll
-    for (int k = 0; k < E; ++k) keep[k] = s[tid + k * NT];
-    run_fft<Tile, NT>(s, tw, a.br_d1, tid);
-    if (a.fbr.active) apply_factor<V, Tile, NT>(s, a.fbr, line0, ncols, tid, toff, eoff, inst);
-    run_fft<Tile, NT>(s, tw, a.br_d2, tid);
-    store_tile<V, Tile, NT>((V*)a.br_out + eoff, s, line0, ncols, tid, false);
-    __syncthreads();
+    for (int k = 0; k < E; ++k) keep[k] = r[k];
+    run_fft<Tile, NT>(r, s, tw, a.br_d1, tid);
+    if (a.fbr.active) apply_factor<V, Tile, NT>(r, a.fbr, lg, pos0, ncols, toff, eoff, inst);
+    run_fft<Tile, NT>(r, s, tw, a.br_d2, tid);
+    store_regs<V, Tile, NT>((V*)a.br_out + eoff, r, lg, pos0, ncols, false);
 #pragma unroll
-    for (int k = 0; k < E; ++k) s[tid + k * NT] = keep[k];
+    for (int k = 0; k < E; ++k) r[k] = keep[k];
   }
 
-  if (a.f2.active) apply_factor<V, Tile, NT>(s, a.f2, line0, ncols, tid, toff, eoff, inst);
-  run_fft<Tile, NT>(s, tw, a.d2, tid);
-  if (a.f3.active) apply_factor<V, Tile, NT>(s, a.f3, line0, ncols, tid, toff, eoff, inst);
-  if (a.out) store_tile<V, Tile, NT>((V*)a.out + eoff, s, line0, ncols, tid, false);
-  if (Tile::IS_ROW && a.red_abs2 && a.abs2_end) row_abs2<V, Tile, NT>(s, a, tid, inst);
-
-  if (!Tile::IS_ROW && (a.red_line || a.red_cross || a.red_sq)) {
-    // deterministic reductions over the column slab (fixed order, no atomics)
-    constexpr int B = Tile::LINES;
-    __shared__ double red[NT];
-    double lsum = 0.0, sq = 0.0;
-#pragma unroll 4
-    for (int k = 0; k < E; ++k) {
-      const int e = tid + k * NT;
-      V v = s[e];
-      const double re = (double)v.x, im = (double)v.y;
-      lsum += re;
-      sq += re * re - im * im;
-      if (a.red_cross) {
-        // the B values of one grid row sit in B consecutive lanes
-        double c = re;
+  if (a.f2.active) apply_factor<V, Tile, NT>(r, a.f2, lg, pos0, ncols, toff, eoff, inst);
+  run_fft<Tile, NT>(r, s, tw, a.d2, tid);
+  if (a.f3.active) apply_factor<V, Tile, NT>(r, a.f3, lg, pos0, ncols, toff, eoff, inst);
+  if (a.out) store_regs<V, Tile, NT>((V*)a.out + eoff, r, lg, pos0, ncols, false);
+  if (Tile::IS_ROW && a.red_abs2 && a.abs2_end) {
+    T acc = T(0);
 #pragma unroll
-        for (int o = B / 2; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o, B);
-        if ((tid & (B - 1)) == 0)
-          a.red_cross[((long long)inst * gridDim.x + blockIdx.x) * a.nrows + e / B] = c;
+    for (int k = 0; k < E; ++k) acc += r[k].x * r[k].x + r[k].y * r[k].y;
+    const double tot = block_sum<NT>((double)acc, red, tid);
+    if (tid == 0) a.red_abs2[(long long)inst * gridDim.x + blockIdx.x] = tot;
+  }
+
+  if constexpr (!Tile::IS_ROW) {
+    constexpr int B = L;
+    // per-thread partials over the thread's E elements of its column (working precision), then
+    // FP64 across threads in a fixed order
+    if (a.col_alt || a.alt_cross) {
+      __shared__ double2 cred[NT];
+      T cr = T(0), ci = T(0);
+#pragma unroll
+      for (int k = 0; k < E; ++k) {
+        const int pos = pos0 + k * STEP;
+        const T re = r[k].x, im = r[k].y;
+        if (pos & 1) {
+          cr -= re;
+          ci -= im;
+        } else {
+          cr += re;
+          ci += im;
+        }
+        if (a.alt_cross) {
+          // across the block's B columns in working precision (B <= 16 terms), FP64 beyond
+          T xr = (lg & 1) ? -re : re, xi = (lg & 1) ? -im : im;
+#pragma unroll
+          for (int o = B / 2; o > 0; o >>= 1) {
+            xr += __shfl_xor_sync(0xffffffffu, xr, o, B);
+            xi += __shfl_xor_sync(0xffffffffu, xi, o, B);
+          }
+          if (line == 0) {
+            if (a.cluster > 1)
+              reinterpret_cast<double2*>(aw_smem + sizeof(V) * Tile::SMEM_ELEMS)[pos] = make_double2((double)xr, (double)xi);
+            else
+              a.alt_cross[((long long)inst * gridDim.x + blockIdx.x) * a.nrows + pos] = make_double2((double)xr, (double)xi);
+          }
+        }
       }
-    }
-    if (a.red_line) {
-      red[tid] = lsum;
-      __syncthreads();
-      if (tid < B) {
-        double acc = 0.0;
-        for (int m = tid; m < NT; m += B) acc += red[m];
-        a.red_line[(long long)inst * ncols + line0 + tid] = acc;
-      }
-      __syncthreads();
-    }
-    if (a.red_sq) {
-      red[tid] = sq;
-      __syncthreads();
-      for (int w = NT / 2; w > 0; w >>= 1) {
-        if (tid < w) red[tid] += red[tid + w];
+      if (a.col_alt) {
+        cred[tid] = make_double2((double)cr, (double)ci);
+        __syncthreads();
+        if (tid < B) {
+          double sr = 0.0, si = 0.0;
+          for (int m = tid; m < NT; m += B) {
+            sr += cred[m].x;
+            si += cred[m].y;
+          }
+          a.col_alt[(long long)inst * ncols + line0 + tid] = make_double2(sr, si);
+        }
         __syncthreads();
       }
-      if (tid == 0) a.red_sq[(long long)inst * gridDim.x + blockIdx.x] = red[0];
+      if (a.alt_cross && a.cluster > 1) {
+        // sum the cluster's per-block row partials through distributed shared memory, rank order
+        cg::cluster_group cl = cg::this_cluster();
+        cl.sync();
+        const int rank = (int)cl.block_rank();
+        const int ncl = (int)cl.num_blocks();
+        const int n = a.nrows;
+        const int lo = rank * (n / ncl), hi = lo + n / ncl;
+        double2* mine = reinterpret_cast<double2*>(aw_smem + sizeof(V) * Tile::SMEM_ELEMS);
+        for (int k = lo + tid; k < hi; k += NT) {
+          double sr = 0.0, si = 0.0;
+          for (int q = 0; q < ncl; ++q) {
+            const double2 v = cl.map_shared_rank(mine, q)[k];
+            sr += v.x;
+            si += v.y;
+          }
+          a.alt_cross[((long long)inst * (gridDim.x / ncl) + blockIdx.x / ncl) * n + k] = make_double2(sr, si);
+        }
+        cl.sync();
+      }
+    }
+    if (a.red_line || a.red_cross || a.red_sq) {
+      double lsum = 0.0, sq = 0.0;
+#pragma unroll
+      for (int k = 0; k < E; ++k) {
+        const int pos = pos0 + k * STEP;
+        const double re = (double)r[k].x, im = (double)r[k].y;
+        lsum += re;
+        sq += re * re - im * im;
+        if (a.red_cross) {
+          double c = re;
+#pragma unroll
+          for (int o = B / 2; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o, B);
+          if (line == 0) a.red_cross[((long long)inst * gridDim.x + blockIdx.x) * a.nrows + pos] = c;
+        }
+      }
+      if (a.red_line) {
+        red[tid] = lsum;
+        __syncthreads();
+        if (tid < B) {
+          double acc = 0.0;
+          for (int m = tid; m < NT; m += B) acc += red[m];
+          a.red_line[(long long)inst * ncols + line0 + tid] = acc;
+        }
+        __syncthreads();
+      }
+      if (a.red_sq) {
+        const double tot = block_sum<NT>(sq, red, tid);
+        if (tid == 0) a.red_sq[(long long)inst * gridDim.x + blockIdx.x] = tot;
+      }
     }
   }
 }
 
 // ------------------------------------------------------------------ dispatch
-template <typename V, int N>
-static int launch_row_n(const AwPassArgs* a, int batch, cudaStream_t st) {
-  typedef typename PassShape<V>::template Row<N> S;
-  typedef RowTile<N, S::L> Tile;
-  if (a->nrows % S::L) return -2;
-  const size_t smem = sizeof(V) * S::TILE;
-  auto kern = aw_pass_kernel<V, Tile, S::NT>;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return -3;
-  }
-  dim3 grid(a->nrows / S::L, batch);
-  kern<<<grid, S::NT, smem, st>>>(*a);
-  return cudaGetLastError() == cudaSuccess ? 0 : -4;
+static constexpr int AW_SMS = 152;
+
+// rows per row-pass block: tiles of about 1024 elements
+inline int choose_row_lines(int ncols, int esz) {
+  int l = 1024 / ncols;
+  if (l < 1) l = 1;
+  return l;
 }
 
-template <typename V, int N>
-static int launch_col_n(const AwPassArgs* a, int batch, cudaStream_t st) {
-  typedef typename PassShape<V>::template Col<N> S;
-  typedef ColTile<N, S::B> Tile;
-  if (a->ncols % S::B) return -2;
-  const size_t smem = sizeof(V) * S::TILE;
-  auto kern = aw_pass_kernel<V, Tile, S::NT>;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return -3;
-  }
-  dim3 grid(a->ncols / S::B, batch);
-  kern<<<grid, S::NT, smem, st>>>(*a);
-  return cudaGetLastError() == cudaSuccess ? 0 : -4;
+// columns per column-pass block: as many as fit (<= 16, <= 128 KB of shared memory) while the
+// launch still has at least 4 blocks per SM
+inline int max_col_lines(int nrows, int ncols, int esz) {
+  int b = 16;
+  while (b > 1 && ((long long)nrows * b * esz > 128 * 1024 || ncols % b)) b >>= 1;
+  return b;
 }
+
+inline int choose_col_lines(int nrows, int ncols, int batch, int esz) {
+  // as many columns as fit while the launch keeps at least 4 blocks per SM
+  int b = 16;
+  while (b > 1 && ((long long)nrows * b * esz > 128 * 1024 || (long long)(ncols / b) * batch < 4 * AW_SMS || ncols % b))
+    b >>= 1;
+  return b;
+}
+
+// Opt a kernel in, once, to the dynamic shared memory its launches can ask for (tile plus, for a
+// clustered column pass, one row of FP64 partials), within the 227 KB per block of sm_103a.
+template <typename K>
+static int prepare_smem(K kern, size_t max_dynamic) {
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess) return -3;
+  const size_t cap = 227 * 1024 - fa.sharedSizeBytes;
+  const size_t want = max_dynamic < cap ? max_dynamic : cap;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want) != cudaSuccess) return -3;
+  return (int)want;
+}
+
+template <typename V, int N, int LINES>
+static int launch_row_t(const AwPassArgs* a, int batch, cudaStream_t st) {
+  typedef Shape<V, N, LINES> S;
+  if constexpr (!S::FITS) {
+    return -5;
+  } else {
+    typedef RowTile<N, LINES> Tile;
+    if (a->nrows % LINES) return -2;
+    const size_t smem = sizeof(V) * Tile::SMEM_ELEMS;
+    auto kern = aw_pass_kernel<V, Tile, S::NT>;
+    static int max_dyn = prepare_smem(kern, smem);
+    if (max_dyn < (int)smem) return -3;
+    dim3 grid(a->nrows / LINES, batch);
+    kern<<<grid, S::NT, smem, st>>>(*a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -4;
+  }
+}
+
+template <typename V, int N, int LINES>
+static int launch_col_t(const AwPassArgs* a, int batch, cudaStream_t st) {
+  typedef Shape<V, N, LINES> S;
+  if constexpr (!S::FITS) {
+    return -5;
+  } else {
+    typedef ColTile<N, LINES> Tile;
+    if (a->ncols % LINES) return -2;
+    const bool clustered = a->alt_cross && a->cluster > 1;
+    // a clustered launch keeps one row of partials (N complex FP64) behind the tile
+    const size_t smem = sizeof(V) * Tile::SMEM_ELEMS + (clustered ? sizeof(double2) * N : 0);
+    auto kern = aw_pass_kernel<V, Tile, S::NT>;
+    static int max_dyn = prepare_smem(kern, sizeof(V) * Tile::SMEM_ELEMS + sizeof(double2) * N);
+    if (max_dyn < (int)smem) return -3;
+    dim3 grid(a->ncols / LINES, batch);
+    if (!clustered) {
+      kern<<<grid, S::NT, smem, st>>>(*a);
+      return cudaGetLastError() == cudaSuccess ? 0 : -4;
+    }
+    if ((a->ncols / LINES) % a->cluster || N % a->cluster || a->cluster > 8) return -6;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(S::NT);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = a->cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, *a);
+    return e == cudaSuccess ? 0 : -4;
+  }
+}
+
+template <typename V, int N> static int launch_row_n(const AwPassArgs* a, int batch, cudaStream_t st) {
+  constexpr int L = 1024 / N >= 1 ? 1024 / N : 1;
+  return launch_row_t<V, N, L>(a, batch, st);
+}
+
+template <typename V, int N> static int launch_col_n(const AwPassArgs* a, int batch, cudaStream_t st) {
+  switch (a->lines_hint ? a->lines_hint : choose_col_lines(a->nrows, a->ncols, batch, (int)sizeof(V))) {
+    case 1: return launch_col_t<V, N, 1>(a, batch, st);
+    case 2: return launch_col_t<V, N, 2>(a, batch, st);
+    case 4: return launch_col_t<V, N, 4>(a, batch, st);
+    case 8: return launch_col_t<V, N, 8>(a, batch, st);
+    case 16: return launch_col_t<V, N, 16>(a, batch, st);
+    default: return -1;
+  }
+}
+
+#define AW_FOR_SIZES(M) M(64) M(128) M(256) M(512) M(1024) M(2048) M(4096) M(8192)
 
 template <typename V> static int launch_row(const AwPassArgs* a, int batch, cudaStream_t st) {
   switch (a->ncols) {
-    case 64: return launch_row_n<V, 64>(a, batch, st);
-    case 128: return launch_row_n<V, 128>(a, batch, st);
-    case 256: return launch_row_n<V, 256>(a, batch, st);
-    case 512: return launch_row_n<V, 512>(a, batch, st);
-    case 1024: return launch_row_n<V, 1024>(a, batch, st);
-    case 2048: return launch_row_n<V, 2048>(a, batch, st);
-    case 4096: return launch_row_n<V, 4096>(a, batch, st);
-    case 8192: return launch_row_n<V, 8192>(a, batch, st);
+#define AW_CASE(NN) \
+  case NN: return launch_row_n<V, NN>(a, batch, st);
+    AW_FOR_SIZES(AW_CASE)
+#undef AW_CASE
     default: return -1;
   }
 }
 
 template <typename V> static int launch_col(const AwPassArgs* a, int batch, cudaStream_t st) {
   switch (a->nrows) {
-    case 64: return launch_col_n<V, 64>(a, batch, st);
-    case 128: return launch_col_n<V, 128>(a, batch, st);
-    case 256: return launch_col_n<V, 256>(a, batch, st);
-    case 512: return launch_col_n<V, 512>(a, batch, st);
-    case 1024: return launch_col_n<V, 1024>(a, batch, st);
-    case 2048: return launch_col_n<V, 2048>(a, batch, st);
-    case 4096: return launch_col_n<V, 4096>(a, batch, st);
-    case 8192: return launch_col_n<V, 8192>(a, batch, st);
-    default: return -1;
-  }
-}
-
-template <typename V> static int row_lines(int ncols) {
-  switch (ncols) {
-#define AW_RL(NN) \
-  case NN: return PassShape<V>::template Row<NN>::L;
-    AW_RL(64) AW_RL(128) AW_RL(256) AW_RL(512) AW_RL(1024) AW_RL(2048) AW_RL(4096) AW_RL(8192)
-#undef AW_RL
-    default: return -1;
-  }
-}
-
-template <typename V> static int col_blocks(int nrows, int ncols) {
-  switch (nrows) {
-#define AW_CB(NN) \
-  case NN: return ncols / PassShape<V>::template Col<NN>::B;
-    AW_CB(64) AW_CB(128) AW_CB(256) AW_CB(512) AW_CB(1024) AW_CB(2048) AW_CB(4096) AW_CB(8192)
-#undef AW_CB
+#define AW_CASE(NN) \
+  case NN: return launch_col_n<V, NN>(a, batch, st);
+    AW_FOR_SIZES(AW_CASE)
+#undef AW_CASE
     default: return -1;
   }
 }

@@ -55,6 +55,11 @@ typedef struct AwPassArgs {
   double* red_line;         // column pass: per column, sum of Re
   double* red_cross;        // column pass: [block][row], sum of Re over the block's columns
   double* red_sq;           // column pass: [block], sum of Re(v*v)
+  double2* col_alt;         // column pass: per column j, Sum_i (-1)^i v_ij (after f3)
+  double2* alt_cross;       // column pass: [block][row i], Sum over the block's columns j of (-1)^j v_ij
+  int lines_hint;           // column pass: columns per block (0: chosen for occupancy)
+  int cluster;              // column pass: blocks per thread-block cluster; > 1 reduces alt_cross across the
+                            // cluster through distributed shared memory ([cluster][row] partials)
   double2* diag_out;        // row pass: element (i, i) at the branch point
   double* red_abs2;         // row pass: [block], sum of |v|^2 at the branch point (or at the end)
   int abs2_end;             // take red_abs2 after f3 instead of at the branch point
@@ -69,8 +74,12 @@ int aw_launch_row_pass_f64(const AwPassArgs* a, int batch, void* stream);
 int aw_launch_col_pass_f64(const AwPassArgs* a, int batch, void* stream);
 int aw_launch_row_pass_f32(const AwPassArgs* a, int batch, void* stream);
 int aw_launch_col_pass_f32(const AwPassArgs* a, int batch, void* stream);
-// number of column blocks (rows of red_cross) the column pass uses for a given N
+// number of column blocks (rows of red_cross) the column pass uses for a given N (single instance)
 int aw_col_pass_blocks(int nrows, int ncols, int f32);
+// columns per column-pass block for `batch` instances
+int aw_col_pass_lines(int nrows, int ncols, int batch, int f32);
+// the most columns a column-pass block can hold (shared-memory limit)
+int aw_col_pass_max_lines(int nrows, int ncols, int f32);
 // number of rows one row-pass block holds for a row length ncols
 int aw_row_pass_lines(int ncols, int f32);
 // number of blocks of a row pass over nrows rows

@@ -203,6 +203,19 @@ __global__ void k_axpy(void* y, const void* x, int f32, long long n, double cr, 
   }
 }
 
+// out[k] = Sum_b part[b][k] in index order (partials of the column-pass cross reductions)
+__global__ void k_sum_parts(const double2* part, int nparts, int n, double2* out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double sr = 0.0, si = 0.0;
+  for (int b = 0; b < nparts; ++b) {
+    const double2 v = part[(long long)b * n + k];
+    sr += v.x;
+    si += v.y;
+  }
+  out[k] = make_double2(sr, si);
+}
+
 __global__ void k_set2(double* p, double a, double b) {
   p[0] = a;
   p[1] = b;
@@ -265,6 +278,10 @@ int aw_k_vdot(const void* a, const void* b, int f32, long long n, double2* part,
 }
 int aw_k_axpy(void* y, const void* x, int f32, long long n, double cr, double ci, void* s) {
   k_axpy<<<grid_for(n), 256, 0, (cudaStream_t)s>>>(y, x, f32, n, cr, ci);
+  return ok();
+}
+int aw_k_sum_parts(const double2* part, int nparts, int n, double2* out, void* s) {
+  k_sum_parts<<<(n + 127) / 128, 128, 0, (cudaStream_t)s>>>(part, nparts, n, out);
   return ok();
 }
 int aw_k_set2(double* p, double a, double b, void* s) {

@@ -15,6 +15,7 @@ int aw_k_psi2rho(const void* psi, int f32, int N, void* rho, void* s);
 int aw_k_trace_finalize(const double2* diag, int n, const double* abs2part, int nparts, double dX, int complex_trace,
                         double* inv_out, double* hist, int* stop, int stop_on_purity, void* s);
 int aw_k_set2(double* p, double a, double b, void* s);
+int aw_k_sum_parts(const double2* part, int nparts, int n, double2* out, void* s);
 int aw_k_norm_finalize(const double* parts, int nparts, double scale, double* inv_out, double* hist, void* s);
 int aw_k_abs2(const void* a, int f32, long long n, double* out, void* s);
 int aw_k_vdot(const void* a, const void* b, int f32, long long n, double2* part, int nblocks, void* s);

@@ -91,6 +91,7 @@ typedef struct aw_config {
   const int32_t* term_index; /* index into obs_x / obs_p */
   const double* term_coef;
   int32_t n_slots;
+  int32_t obs_p_time_dependent; /* a P-only observable mentions t */
 } aw_config;
 
 /* library */

@@ -136,3 +136,20 @@ def test_wigner_bloch_ground_state():
     Wc = c.get_ground_state(abs_tol_purity=1e-8)
     assert rel_l2(Wg, Wc) < 1e-8
     assert abs(g.get_average(g.hamiltonian) - 0.5) < 1e-4
+
+
+def test_large_grid_marginal_pass_1024():
+    """1024 x 1024 exercises the clustered marginal column pass (48 KB shared memory per block)."""
+    from accuratewigner_gb300 import WignerMoyalCUDA1D
+    from oracle.propagators import WignerMoyalOracle
+
+    p = dict(WM_ANHARMONIC, X_gridDIM=1024, P_gridDIM=1024, X_amplitude=12.0, P_amplitude=12.0)
+    g = WignerMoyalCUDA1D(**p)
+    c = WignerMoyalOracle(**p)
+    g.set_wignerfunction(WM_INIT)
+    c.set_wignerfunction(WM_INIT)
+    g.propagate(3)
+    c.propagate(3)
+    assert rel_l2(g.wignerfunction.get(), c.wignerfunction) < TOL
+    for name in ("X_average", "P_average", "P_average_RHS", "hamiltonian_average"):
+        assert obs_close(getattr(g, name), getattr(c, name), TOL), name
