@@ -1,0 +1,24 @@
+"""The GPU library against golden vectors made by the reference's own kernel code."""
+import pytest
+
+from golden_cases import CASES, compare, load_golden, run_ops
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10  # plain complex128 form
+
+
+def _gpu_cls(kind):
+    import accuratewigner_gb300 as aw
+
+    return {"wm": aw.WignerMoyalCUDA1D, "wb": aw.WignerBlochCUDA1D, "vn": aw.RhoVNeumannCUDA1D,
+            "rb": aw.RhoBlochCUDA1D, "sw": aw.SchrodingerWignerCUDA1D}[kind]
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_gpu_matches_reference_kernels(name):
+    spec = CASES[name]
+    obj = _gpu_cls(spec["kind"])(**spec["params"])
+    got = run_ops(obj, spec)
+    bad = compare(got, load_golden(name), TOL)
+    assert not bad, bad
