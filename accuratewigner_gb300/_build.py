@@ -1,6 +1,6 @@
 """Build recipe of libawigner.so (sm_103a), in-tree.
 
-Four translation units are compiled in parallel with nvcc for sm_103a and
+The translation units are compiled in parallel with nvcc for sm_103a and
 linked into ``accuratewigner_gb300/libawigner.so``; NVRTC (dynamic) compiles
 the user-expression modules at run time.  Objects go to ``_build/`` at the
 repository root.  Rebuilds only what is out of date.
@@ -17,7 +17,10 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libawigner.so")
 
-SOURCES = ["aw_api.cu", "aw_util.cu", "aw_pass_f64.cu", "aw_pass_f32.cu", "aw_noalloc.cu"]
+# the double-float pass kernels are the slowest to compile: one unit per line length, started first
+DF_SIZES = [32, 64, 128, 256, 512, 1024, 2048, 4096, 8192]
+SOURCES = (["aw_pass_df_%d.cu" % n for n in DF_SIZES] +
+           ["aw_api.cu", "aw_util.cu", "aw_pass_f64.cu", "aw_pass_f32.cu", "aw_pass_df.cu", "aw_noalloc.cu"])
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 

@@ -156,13 +156,28 @@ class TermTable:
         cfg.obs_p_time_dependent = int(any(self.info.depends_on(e, "t") for e in self.obs_p))
 
 
+# precision of propagators constructed without the keyword
+DEFAULT_PRECISION = "c128"
+
+
 def precision_code(kwargs):
-    p = kwargs.get("precision", "c128")
-    if p in ("c128", "complex128", np.complex128, _lib.AW_C128):
-        return _lib.AW_C128
-    if p in ("c64", "complex64", np.complex64, _lib.AW_C64):
-        return _lib.AW_C64
-    raise ValueError("precision must be 'c128' or 'c64'")
+    """State and arithmetic of the passes.
+
+    'c128' (default): complex128 state, passes in double-float arithmetic on the FP32 pipes.
+    'c128-fp64': complex128 state, passes in native FP64 arithmetic.
+    'c64': complex64 state and passes, FP64 tables and reductions.
+    """
+    p = kwargs.get("precision", DEFAULT_PRECISION)
+    if isinstance(p, str) or p in (np.complex128, np.complex64):
+        if p in ("c128", "complex128", np.complex128):
+            return _lib.AW_C128
+        if p in ("c128-fp64", "fp64"):
+            return _lib.AW_C128_FP64
+        if p in ("c64", "complex64", np.complex64):
+            return _lib.AW_C64
+    elif p in (_lib.AW_C128, _lib.AW_C64, _lib.AW_C128_FP64):
+        return int(p)
+    raise ValueError("precision must be 'c128', 'c128-fp64' or 'c64'")
 
 
 def mask_mode(info, expr):

@@ -26,6 +26,7 @@ AW_SCHRODINGER = 4
 
 AW_C128 = 0
 AW_C64 = 1
+AW_C128_FP64 = 2
 
 AW_BUF_RHO = 0
 AW_BUF_WIGNER = 1

@@ -136,6 +136,9 @@ struct aw_state_s {
   std::vector<double> tcoef;
   awjit::KindNames kn;
   int kind = 0, f32 = 0, esz = 16;
+  int df = 0;                          // complex128 state, passes in double-float arithmetic
+  // buffers currently holding double-float state (pointer, elements); plain complex128 at rest
+  std::vector<std::pair<void*, long long>> df_live;
   int nr = 0, nc = 0;      // main grid rows x cols
   int wn = 0;              // Wigner grid side (VN: 2N; SW: N; WM: same as main)
   cudaStream_t st = nullptr;
@@ -267,8 +270,34 @@ static double define_round(double v) {
   return strtod(buf, nullptr);
 }
 
+// Element format of the tables the passes read: 0 FP64, 1 FP32, 2 double-float
+// (each FP64 number as the FP32 pair hi = rn(v), lo = rn(v - hi)).
+static int tab_fmt(const aw_state_s* h) { return h->f32 ? 1 : (h->df ? 2 : 0); }
+
+// upload real numbers (interleaved re, im for complex tables) in table format fmt
+static int upload_reals(DevBuf& dst, const std::vector<double>& v, int fmt) {
+  const size_t n = v.size();
+  TRY(dalloc(dst, n * (fmt == 1 ? 4 : 8)));
+  if (n == 0) return AW_OK;
+  if (fmt == 0) {
+    CK(cudaMemcpy(dst.p, v.data(), n * 8, cudaMemcpyHostToDevice));
+  } else if (fmt == 1) {
+    std::vector<float> g(v.begin(), v.end());
+    CK(cudaMemcpy(dst.p, g.data(), n * 4, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> g(2 * n);
+    for (size_t k = 0; k < n; ++k) {
+      const float hi = (float)v[k];
+      g[2 * k] = hi;
+      g[2 * k + 1] = (float)(v[k] - (double)hi);
+    }
+    CK(cudaMemcpy(dst.p, g.data(), n * 8, cudaMemcpyHostToDevice));
+  }
+  return AW_OK;
+}
+
 // twiddle table tw[m] = exp(-2 pi i m / n), built in extended precision
-static int make_twiddles(DevBuf& dst, int n, int f32) {
+static int make_twiddles(DevBuf& dst, int n, int fmt) {
   const long double PI = 3.141592653589793238462643383279502884L;
   std::vector<double> h(2 * (size_t)n);
   for (int m = 0; m < n; ++m) {
@@ -290,21 +319,14 @@ static int make_twiddles(DevBuf& dst, int n, int f32) {
     h[2 * m] = (double)c;
     h[2 * m + 1] = (double)s;
   }
-  TRY(dalloc(dst, (size_t)n * (f32 ? 8 : 16)));
-  if (f32) {
-    std::vector<float> g(2 * (size_t)n);
-    for (size_t k = 0; k < g.size(); ++k) g[k] = (float)h[k];
-    CK(cudaMemcpy(dst.p, g.data(), g.size() * 4, cudaMemcpyHostToDevice));
-  } else {
-    CK(cudaMemcpy(dst.p, h.data(), h.size() * 8, cudaMemcpyHostToDevice));
-  }
+  TRY(upload_reals(dst, h, fmt));
   return AW_OK;
 }
 
 // Two-level table of a bilinear phase exp(i alpha_line (q - npos/2)) * norm
 // for q = 0..npos-1, split as hi[q / lo] * lo[q % lo].
 static int make_shear(DevBuf& hi, DevBuf& lo, int* lo_n, const std::vector<double>& alpha, int npos, double norm,
-                      int f32, double offset = -1.0) {
+                      int fmt, double offset = -1.0) {
   if (offset < 0) offset = 0.5 * npos;
   const int LO = npos < 32 ? npos : 32;
   const int nhi = npos / LO;
@@ -323,23 +345,14 @@ static int make_shear(DevBuf& hi, DevBuf& lo, int* lo_n, const std::vector<doubl
       L[2 * ((size_t)ln * LO + l) + 1] = sin(ph);
     }
   }
-  const size_t es = f32 ? 8 : 16;
-  TRY(dalloc(hi, (size_t)lines * nhi * es));
-  TRY(dalloc(lo, (size_t)lines * LO * es));
-  if (f32) {
-    std::vector<float> h2(H.begin(), H.end()), l2(L.begin(), L.end());
-    CK(cudaMemcpy(hi.p, h2.data(), h2.size() * 4, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(lo.p, l2.data(), l2.size() * 4, cudaMemcpyHostToDevice));
-  } else {
-    CK(cudaMemcpy(hi.p, H.data(), H.size() * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(lo.p, L.data(), L.size() * 8, cudaMemcpyHostToDevice));
-  }
+  TRY(upload_reals(hi, H, fmt));
+  TRY(upload_reals(lo, L, fmt));
   *lo_n = LO;
   return AW_OK;
 }
 
 // exp(2 pi i (line * q mod n) / n) / n split as hi[q / lo] * lo[q % lo], exact integer reduction
-static int make_twist(DevBuf& hi, DevBuf& lo, int* lo_n, int n, int f32) {
+static int make_twist(DevBuf& hi, DevBuf& lo, int* lo_n, int n, int fmt) {
   const int LO = n < 32 ? n : 32;
   const int nhi = n / LO;
   const long double PI = 3.141592653589793238462643383279502884L;
@@ -358,17 +371,8 @@ static int make_twist(DevBuf& hi, DevBuf& lo, int* lo_n, int n, int f32) {
       L[2 * ((size_t)ln * LO + l) + 1] = (double)sinl(a);
     }
   }
-  const size_t es = f32 ? 8 : 16;
-  TRY(dalloc(hi, (size_t)n * nhi * es));
-  TRY(dalloc(lo, (size_t)n * LO * es));
-  if (f32) {
-    std::vector<float> h2(H.begin(), H.end()), l2(L.begin(), L.end());
-    CK(cudaMemcpy(hi.p, h2.data(), h2.size() * 4, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(lo.p, l2.data(), l2.size() * 4, cudaMemcpyHostToDevice));
-  } else {
-    CK(cudaMemcpy(hi.p, H.data(), H.size() * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(lo.p, L.data(), L.size() * 8, cudaMemcpyHostToDevice));
-  }
+  TRY(upload_reals(hi, H, fmt));
+  TRY(upload_reals(lo, L, fmt));
   *lo_n = LO;
   return AW_OK;
 }
@@ -402,24 +406,75 @@ static double pass_bytes(const aw_state_s* h, const AwPassArgs& a) {
   return n * acc * h->esz;
 }
 
-static int row_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw) {
-  a.tw = tw.p;
-  cudaEvent_t pe = prof_mark(h);
-  int r = h->f32 ? aw_launch_row_pass_f32(&a, 1, h->st) : aw_launch_row_pass_f64(&a, 1, h->st);
-  prof_done(h, PROF_ROW, pass_bytes(h, a), pe);
-  ++g_launches;
-  if (r) return fail(AW_E_CUDA, "row pass launch failed (%d, %s), grid %d x %d", r, cudaGetErrorString(cudaGetLastError()), a.nrows, a.ncols);
+// Double-float state tracking.  With h->df the passes read and write state in the double-float
+// form; buffers are converted on their first use by a pass (in place, or into the pass's output
+// when it writes elsewhere, so that an input buffer is never altered) and converted back to
+// complex128 by settle() before any other kernel or the caller sees them.
+static bool df_is_live(const aw_state_s* h, const void* p) {
+  for (auto& e : h->df_live)
+    if (e.first == p) return true;
+  return false;
+}
+static void df_mark(aw_state_s* h, void* p, long long n) {
+  if (!p) return;
+  for (auto& e : h->df_live)
+    if (e.first == p) {
+      e.second = std::max(e.second, n);
+      return;
+    }
+  h->df_live.push_back({p, n});
+}
+static int settle(aw_state_s* h) {
+  for (auto& e : h->df_live) KL(aw_k_convert(e.first, 2, e.first, 0, e.second, h->st));
+  h->df_live.clear();
   return AW_OK;
 }
-static int col_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw) {
-  a.tw = tw.p;
-  cudaEvent_t pe = prof_mark(h);
-  int r = h->f32 ? aw_launch_col_pass_f32(&a, 1, h->st) : aw_launch_col_pass_f64(&a, 1, h->st);
-  prof_done(h, PROF_COL, pass_bytes(h, a), pe);
-  ++g_launches;
-  if (r) return fail(AW_E_CUDA, "column pass launch failed (%d, %s), grid %d x %d", r, cudaGetErrorString(cudaGetLastError()), a.nrows, a.ncols);
+// converts back to complex128 when the scope ends (exported entry points that run passes)
+struct Settled {
+  aw_state_s* h;
+  ~Settled() {
+    if (h && !h->df_live.empty()) settle(h);
+  }
+};
+
+static int df_prepare(aw_state_s* h, AwPassArgs& a) {
+  const long long n = (long long)a.nrows * a.ncols;
+  if (a.in && !df_is_live(h, a.in)) {
+    void* dst = a.out ? a.out : (void*)a.in;
+    KL(aw_k_convert(a.in, 0, dst, 2, n, h->st));
+    a.in = dst;
+    df_mark(h, dst, n);
+  }
   return AW_OK;
 }
+static void df_outputs(aw_state_s* h, const AwPassArgs& a) {
+  const long long n = (long long)a.nrows * a.ncols;
+  df_mark(h, a.out, n);
+  df_mark(h, a.mid_out, n);
+  df_mark(h, a.br_out, n);
+}
+
+static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row) {
+  a.tw = tw.p;
+  if (h->df) TRY(df_prepare(h, a));
+  cudaEvent_t pe = prof_mark(h);
+  int r;
+  if (h->df)
+    r = row ? aw_launch_row_pass_df(&a, 1, h->st) : aw_launch_col_pass_df(&a, 1, h->st);
+  else if (h->f32)
+    r = row ? aw_launch_row_pass_f32(&a, 1, h->st) : aw_launch_col_pass_f32(&a, 1, h->st);
+  else
+    r = row ? aw_launch_row_pass_f64(&a, 1, h->st) : aw_launch_col_pass_f64(&a, 1, h->st);
+  prof_done(h, row ? PROF_ROW : PROF_COL, pass_bytes(h, a), pe);
+  ++g_launches;
+  if (r)
+    return fail(AW_E_CUDA, "%s pass launch failed (%d, %s), grid %d x %d", row ? "row" : "column", r,
+                cudaGetErrorString(cudaGetLastError()), a.nrows, a.ncols);
+  if (h->df) df_outputs(h, a);
+  return AW_OK;
+}
+static int row_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw) { return launch_pass(h, a, tw, true); }
+static int col_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw) { return launch_pass(h, a, tw, false); }
 
 // phase table slots
 enum { TAB_V1 = 0, TAB_V1B, TAB_V2, TAB_K, TAB_BV, TAB_BK, TAB_BLK, TAB_NSLOT };
@@ -445,7 +500,7 @@ static int build_tab(aw_state_s* h, int slot, int fn, int mode, double ta, doubl
   }
   void* col = tab_col(h, slot);
   void* row = tab_row(h, slot);
-  int f32 = h->f32;
+  int f32 = tab_fmt(h);
   void* args[] = {&col, &row, &f32, &fn, &mode, &ncol, &dcol, &roll, &nrow, &drow,
                   &ta, &tb, &ca, &cb, &shift, &maskpow, &tmask};
   const int n = ncol + nrow;
@@ -455,7 +510,7 @@ static int build_tab(aw_state_s* h, int slot, int fn, int mode, double ta, doubl
 static int build_mask2d(aw_state_s* h, int which, double t) {
   DevBuf& m = which == 0 ? h->maskx : h->maskp;
   void* out = m.p;
-  int f32 = h->f32, nr = h->nr, nc = h->nc;
+  int f32 = tab_fmt(h), nr = h->nr, nc = h->nc;
   double a = h->cfg.dXX, b = h->cfg.dXX_prime, c = h->cfg.dPP, d = h->cfg.dPP_prime;
   void* args[] = {&out, &f32, &which, &t, &nr, &nc, &a, &b, &c, &d};
   return hjit(h, h->k_mask2d, dim3((nc + 127) / 128, nr), dim3(128), args);
@@ -493,7 +548,11 @@ static std::string cstr(const char* s, const char* dflt) { return s ? std::strin
 static int create_impl(const aw_config* cfg, aw_state_s* h) {
   h->cfg = *cfg;
   h->kind = cfg->kind;
+  if (cfg->precision < AW_C128 || cfg->precision > AW_C128_FP64) return fail(AW_E_ARG, "unknown precision %d", cfg->precision);
   h->f32 = cfg->precision == AW_C64;
+  // complex128 runs its passes in double-float arithmetic unless native FP64 is asked for; the
+  // one-dimensional Schrodinger propagator keeps FP64 (its passes are launch-bound, not FP64-bound)
+  h->df = cfg->precision == AW_C128 && cfg->kind != AW_SCHRODINGER;
   h->esz = h->f32 ? 8 : 16;
   h->consts = cstr(cfg->cuda_consts, "");
   h->V = cstr(cfg->V, "0.");
@@ -531,8 +590,8 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
     if (h->sw_rows <= 0) return fail(AW_E_ARG, "unsupported wave-function length %d", N);
   }
   const int maxn = h->kn.sw ? 8192 : 8192;
-  if (h->nc < 64 || h->nc > maxn || (!h->kn.sw && (h->nr < 64 || h->nr > maxn)) || (h->wn && h->wn > 8192))
-    return fail(AW_E_ARG, "grid sides must be powers of two in [64, %d] (Wigner grid up to 8192)", maxn);
+  if (h->nc < 32 || h->nc > maxn || (!h->kn.sw && (h->nr < 32 || h->nr > maxn)) || (h->wn && h->wn > 8192))
+    return fail(AW_E_ARG, "grid sides must be powers of two in [32, %d] (Wigner grid up to 8192)", maxn);
 
   CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
 
@@ -577,9 +636,9 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   }
 
   // twiddles
-  TRY(make_twiddles(h->tw_r, h->nc, h->f32));
-  if (!h->kn.sw) TRY(make_twiddles(h->tw_c, h->nr, h->f32));
-  if (h->wn) TRY(make_twiddles(h->tw_w, h->wn, h->f32));
+  TRY(make_twiddles(h->tw_r, h->nc, tab_fmt(h)));
+  if (!h->kn.sw) TRY(make_twiddles(h->tw_c, h->nr, tab_fmt(h)));
+  if (h->wn) TRY(make_twiddles(h->tw_w, h->wn, tab_fmt(h)));
 
   // shear tables of the Wigner transform
   const double a_shx = tan(M_PI / 8.0);   // phase_shearX: a = tan(theta / 2)
@@ -590,27 +649,27 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
     std::vector<double> ax(h->nr), ay(h->nc);
     for (int i = 0; i < h->nr; ++i) ax[i] = -a_shx * cfg->dPP * (cfg->dXX_prime * ((double)i - 0.5 * h->nr));
     for (int j = 0; j < h->nc; ++j) ay[j] = -b_shy * cfg->dPP_prime * (cfg->dXX * ((double)j - 0.5 * h->nc));
-    TRY(make_shear(h->shx_hi, h->shx_lo, &h->shx_lo_n, ax, h->nc, 1.0 / h->nc, h->f32));
-    TRY(make_shear(h->shy_hi, h->shy_lo, &h->shy_lo_n, ay, h->nr, 1.0 / h->nr, h->f32));
+    TRY(make_shear(h->shx_hi, h->shx_lo, &h->shx_lo_n, ax, h->nc, 1.0 / h->nc, tab_fmt(h)));
+    TRY(make_shear(h->shy_hi, h->shy_lo, &h->shy_lo_n, ay, h->nr, 1.0 / h->nr, tab_fmt(h)));
   } else if (h->kn.vn) {
     // rho_vneumann_cuda_1d.py:608-639 on the padded (2N)^2 grid, dXX = dX
     const int M = h->wn;
     std::vector<double> ax(M), ay(M);
     for (int i = 0; i < M; ++i) ax[i] = -a_shx * cfg->dPP * (cfg->dX * ((double)i - 0.5 * M));
     for (int j = 0; j < M; ++j) ay[j] = -b_shy * cfg->dPP * (cfg->dX * ((double)j - 0.5 * M));
-    TRY(make_shear(h->shx_hi, h->shx_lo, &h->shx_lo_n, ax, M, 1.0 / M, h->f32));
-    TRY(make_shear(h->shy_hi, h->shy_lo, &h->shy_lo_n, ay, M, 1.0 / M, h->f32));
+    TRY(make_shear(h->shx_hi, h->shx_lo, &h->shx_lo_n, ax, M, 1.0 / M, tab_fmt(h)));
+    TRY(make_shear(h->shy_hi, h->shy_lo, &h->shy_lo_n, ay, M, 1.0 / M, tab_fmt(h)));
   } else {
     // schrodinger_wigner_cuda_1d.py:695-726: P is fft-shifted along the sheared axis
     const int M = h->wn;
     std::vector<double> ax(M), ay(M);
     for (int i = 0; i < M; ++i) ax[i] = -a_shx * cfg->dP * (cfg->dX * ((double)i - 0.5 * M));
     for (int j = 0; j < M; ++j) ay[j] = -b_shy * cfg->dP * (cfg->dX * ((double)j - 0.5 * M));
-    TRY(make_shear(h->shx_hi, h->shx_lo, &h->shx_lo_n, ax, M, 1.0 / M, h->f32));
-    TRY(make_shear(h->shy_hi, h->shy_lo, &h->shy_lo_n, ay, M, 1.0 / M, h->f32));
+    TRY(make_shear(h->shx_hi, h->shx_lo, &h->shx_lo_n, ax, M, 1.0 / M, tab_fmt(h)));
+    TRY(make_shear(h->shy_hi, h->shy_lo, &h->shy_lo_n, ay, M, 1.0 / M, tab_fmt(h)));
   }
 
-  if (h->kn.vn) TRY(make_twist(h->twist_hi, h->twist_lo, &h->twist_lo_n, h->nc, h->f32));
+  if (h->kn.vn) TRY(make_twist(h->twist_hi, h->twist_lo, &h->twist_lo_n, h->nc, tab_fmt(h)));
 
   // reduction scratch of the Wigner column pass
   const int wr = h->kn.rotated ? h->nr : h->wn, wc = h->kn.rotated ? h->nc : h->wn;
@@ -926,13 +985,7 @@ static int ensure_blackman(aw_state_s* h, int nr, int nc) {
     const double Ci = i * 2.0 * M_PI / (nr - 1.0);
     t[2 * (nc + i)] = 0.42 - 0.5 * cos(Ci) + 0.08 * cos(2.0 * Ci);
   }
-  TRY(dalloc(h->blk_tabs, t.size() / 2 * h->esz));
-  if (h->f32) {
-    std::vector<float> g(t.begin(), t.end());
-    CK(cudaMemcpy(h->blk_tabs.p, g.data(), g.size() * 4, cudaMemcpyHostToDevice));
-  } else {
-    CK(cudaMemcpy(h->blk_tabs.p, t.data(), t.size() * 8, cudaMemcpyHostToDevice));
-  }
+  TRY(upload_reals(h->blk_tabs, t, tab_fmt(h)));
   return AW_OK;
 }
 
@@ -1093,6 +1146,7 @@ static int wm_normalize(aw_state_s* h, double* hist_row) {
   WignerGrid g{h->W.p, h->nr, h->nc, &h->tw_r, &h->tw_c};
   TRY(wigner_passes(h, g, h->rho.p, fsign(), false, true, true));
   TRY(launch_finalize(h, 0.0, hist_row, 0));
+  TRY(settle(h));
   KL(aw_k_scale(h->W.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
   KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
   return AW_OK;
@@ -1100,12 +1154,14 @@ static int wm_normalize(aw_state_s* h, double* hist_row) {
 
 extern "C" int aw_wigner2rho(aw_handle h) {
   if (!h) return fail(AW_E_ARG, "null handle");
+  Settled guard{h};
   if (!h->kn.rotated) return fail(AW_E_STATE, "wigner2rho exists for the Wigner-Moyal / Wigner-Bloch propagators");
   return wm_wigner2rho(h);
 }
 
 extern "C" int aw_normalize_rho_wigner(aw_handle h) {
   if (!h) return fail(AW_E_ARG, "null handle");
+  Settled guard{h};
   if (!h->kn.rotated) return fail(AW_E_STATE, "normalize_rho_wigner exists for the Wigner-Moyal propagators");
   TRY(ensure_hist(h, 1));
   return wm_normalize(h, (double*)h->hist.p);
@@ -1116,6 +1172,7 @@ static int sw_get_wigner(aw_state_s* h, int blackman);
 
 extern "C" int aw_rho2wigner(aw_handle h, int32_t blackman) {
   if (!h) return fail(AW_E_ARG, "null handle");
+  Settled guard{h};
   if (h->kn.rotated) {
     if (blackman) TRY(ensure_blackman(h, h->nr, h->nc));
     WignerGrid g{h->W.p, h->nr, h->nc, &h->tw_r, &h->tw_c};
@@ -1301,6 +1358,7 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
 extern "C" int aw_propagate(aw_handle h, int64_t steps, double* t) {
   if (!h || !t) return fail(AW_E_ARG, "null argument");
   if (steps < 0) return fail(AW_E_ARG, "negative step count");
+  Settled guard{h};
   int vn_propagate(aw_state_s*, long long, double*);
   int sw_propagate(aw_state_s*, long long, double*);
   if (h->kn.vn) return vn_propagate(h, steps, t);
@@ -1318,6 +1376,7 @@ extern "C" int aw_propagate(aw_handle h, int64_t steps, double* t) {
   TRY(rot_run(h, p, steps, times, (double*)h->hist.p));
   if (c.ehrenfest) {
     // the last step's normalisation, applied to both arrays
+    TRY(settle(h));
     KL(aw_k_scale(h->W.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
     KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
     h->hist_rows = steps;
@@ -1394,6 +1453,7 @@ extern "C" int aw_purity(aw_handle h, double* out) {
 // ============================================================================ Bloch
 extern "C" int aw_bloch_step(aw_handle h, double dbeta, double* out) {
   if (!h) return fail(AW_E_ARG, "null handle");
+  Settled guard{h};
   int vn_bloch_step(aw_state_s*, double, double*);
   if (h->kind == AW_RHO_BLOCH) return vn_bloch_step(h, dbeta, out);
   if (h->kind != AW_WIGNER_BLOCH) return fail(AW_E_STATE, "Bloch steps need a Bloch propagator");
@@ -1401,6 +1461,7 @@ extern "C" int aw_bloch_step(aw_handle h, double dbeta, double* out) {
   StepPlan p{true, dbeta, true, false, 0};
   std::vector<double> times(3, 0.0);
   TRY(rot_run(h, p, 1, times, (double*)h->hist.p));
+  TRY(settle(h));
   KL(aw_k_scale(h->W.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
   KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
   if (out) {
@@ -1412,6 +1473,7 @@ extern "C" int aw_bloch_step(aw_handle h, double dbeta, double* out) {
 
 extern "C" int aw_gibbs(aw_handle h, double dbeta, int64_t steps, int64_t* done, double* purity) {
   if (!h) return fail(AW_E_ARG, "null handle");
+  Settled guard{h};
   int vn_gibbs(aw_state_s*, double, long long, long long*, double*);
   if (h->kind == AW_RHO_BLOCH) {
     long long d = 0;
@@ -1445,11 +1507,13 @@ extern "C" int aw_gibbs(aw_handle h, double dbeta, int64_t steps, int64_t* done,
   if (done) *done = ran;
   if (purity && ran > 0) *purity = hh[(size_t)(ran - 1) * cols + cols - 2];
   // rho_n of the last executed step (position representation, unnormalised) and its W
+  TRY(settle(h));
   CK(cudaMemcpyAsync(h->rho.p, h->snap.p, (size_t)h->nr * h->nc * h->esz, cudaMemcpyDeviceToDevice, h->st));
   {
     WignerGrid g{h->W.p, h->nr, h->nc, &h->tw_r, &h->tw_c};
     TRY(wigner_passes(h, g, h->rho.p, fsign(), false, false, true));
   }
+  TRY(settle(h));
   KL(aw_k_scale(h->W.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
   KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
   CK(cudaStreamSynchronize(h->st));
@@ -1591,6 +1655,7 @@ int vn_propagate(aw_state_s* h, long long steps, double* t) {
   if (steps == 0) return AW_OK;
   VnPlan p{false, 0.0, c.ehrenfest != 0, false, 0, 0};
   TRY(vn_run(h, p, steps, times, c.ehrenfest ? (double*)h->hist.p : nullptr, h->hist_cols));
+  TRY(settle(h));
   KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
   h->hist_rows = c.ehrenfest ? steps : 0;
   *t = times[steps];
@@ -1609,6 +1674,7 @@ int vn_bloch_step(aw_state_s* h, double dbeta, double* out) {
     KL(aw_k_trace_finalize((const double2*)h->diag.p, h->nc, (const double*)h->abs2.p,
                            aw_row_pass_blocks(h->nr, h->nc, h->f32), h->cfg.dX, 1, dscal(h, 2),
                            (double*)h->hist.p + h->hist_cols, nullptr, 0, h->st));
+  TRY(settle(h));
   KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
   if (out) {
     std::vector<double> hh(2 * (size_t)h->hist_cols);
@@ -1644,6 +1710,7 @@ int vn_gibbs(aw_state_s* h, double dbeta, long long steps, long long* done, doub
   }
   *done = ran;
   if (purity && ran > 0) *purity = hh[(size_t)(ran - 1) * hc];
+  TRY(settle(h));
   CK(cudaMemcpyAsync(h->rho.p, h->snap.p, (size_t)h->nr * h->nc * h->esz, cudaMemcpyDeviceToDevice, h->st));
   KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
   CK(cudaStreamSynchronize(h->st));
@@ -1659,6 +1726,7 @@ static int vn_get_wigner(aw_state_s* h, int blackman) {
   if (blackman) TRY(ensure_blackman(h, M, M));
   WignerGrid g{h->W.p, M, M, &h->tw_w, &h->tw_w};
   TRY(wigner_passes(h, g, h->W.p, fsign(), blackman != 0, false, true));
+  TRY(settle(h));
   double s[2];
   TRY(dsum(h, h->W.p, (long long)M * M, 0, 0, s));
   KL(aw_k_scale(h->W.p, h->f32, (long long)M * M, 1.0 / (s[0] * h->cfg.dXdP), 0.0, nullptr, h->st));
@@ -1668,6 +1736,7 @@ static int vn_get_wigner(aw_state_s* h, int blackman) {
 extern "C" int aw_average_ops(aw_handle h, const char* const* ops, int32_t n_ops, double t, double* out) {
   if (!h || !out) return fail(AW_E_ARG, "null argument");
   if (!h->kn.vn) return fail(AW_E_STATE, "ordered operator averages are defined for density matrices");
+  Settled guard{h};
   const long long n = (long long)h->nr * h->nc;
   CK(cudaMemcpyAsync(h->tmp.p, h->rho.p, n * h->esz, cudaMemcpyDeviceToDevice, h->st));
   bool is_x = false;
@@ -1682,6 +1751,7 @@ extern "C" int aw_average_ops(aw_handle h, const char* const* ops, int32_t n_ops
     double dX = h->cfg.dX, dP = h->cfg.dP;
     void* args[] = {&buf, &f32, &t, &unused, &nr, &nc, &dX, &dP};
     if (is_x) {
+      TRY(settle(h));
       TRY(hjit(h, kern, dim3((nc + 127) / 128, nr), dim3(128), args));
     } else {
       // sign flip, fft1, / N, observable, ifft1, sign flip (rho_vneumann_cuda_1d.py:549-561)
@@ -1693,6 +1763,7 @@ extern "C" int aw_average_ops(aw_handle h, const char* const* ops, int32_t n_ops
       a.f1.scale = 1.0 / nc;
       a.f1.active = 1;
       TRY(row_pass(h, a, h->tw_r));
+      TRY(settle(h));
       TRY(hjit(h, kern, dim3((nc + 127) / 128, nr), dim3(128), args));
       a = pnone(h);
       a.in = a.out = h->tmp.p;
@@ -1701,6 +1772,7 @@ extern "C" int aw_average_ops(aw_handle h, const char* const* ops, int32_t n_ops
       TRY(row_pass(h, a, h->tw_r));
     }
   }
+  TRY(settle(h));
   double s[2];
   TRY(dsum(h, h->tmp.p, h->nr, 3, h->nc + 1, s));
   *out = s[0] * h->cfg.dX;

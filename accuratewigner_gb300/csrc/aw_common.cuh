@@ -2,10 +2,14 @@
 //
 // The reference keeps every state in pycuda::complex<double>
 // (wigner_moyal_cuda_1d.py:629); here a state element is a CUDA vector type:
-// double2 for the plain complex128 form and float2 for the complex64 form.
+// double2 for the native complex128 form, float2 for the complex64 form and
+// dfc (a double-float complex of four FP32 numbers, also 16 bytes) for the
+// complex128 form computed on the FP32 pipes.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include "aw_df.cuh"
 
 template <typename T> struct cvec;
 template <> struct cvec<double> { typedef double2 type; };
@@ -14,6 +18,43 @@ template <> struct cvec<float> { typedef float2 type; };
 template <typename V> struct scalar_of;
 template <> struct scalar_of<double2> { typedef double type; };
 template <> struct scalar_of<float2> { typedef float type; };
+template <> struct scalar_of<dfc> { typedef dfr type; };
+
+// double-float scalar operators, so that the element-wise code is written once
+__device__ __forceinline__ dfr operator+(dfr a, dfr b) { return df_add(a, b); }
+__device__ __forceinline__ dfr operator-(dfr a, dfr b) { return df_sub(a, b); }
+__device__ __forceinline__ dfr operator-(dfr a) { return df_neg(a); }
+__device__ __forceinline__ dfr operator*(dfr a, dfr b) { return df_mul(a, b); }
+__device__ __forceinline__ dfr& operator*=(dfr& a, dfr b) { return a = df_mul(a, b); }
+__device__ __forceinline__ dfr& operator+=(dfr& a, dfr b) { return a = df_add(a, b); }
+__device__ __forceinline__ dfr& operator-=(dfr& a, dfr b) { return a = df_sub(a, b); }
+__device__ __forceinline__ bool operator==(dfr a, dfr b) { return a.h == b.h && a.l == b.l; }
+
+// scalar conversions
+template <typename T> __device__ __forceinline__ T from_double(double v) { return (T)v; }
+template <> __device__ __forceinline__ dfr from_double<dfr>(double v) { return df_from_double(v); }
+__device__ __forceinline__ double to_d(double v) { return v; }
+__device__ __forceinline__ double to_d(float v) { return (double)v; }
+__device__ __forceinline__ double to_d(dfr v) { return df_to_double(v); }
+
+// lanes of a warp that exist in a block of NT threads
+template <int NT> __device__ __forceinline__ unsigned lane_mask() { return NT >= 32 ? 0xffffffffu : (1u << NT) - 1u; }
+
+// warp shuffles of a scalar over the lanes in m
+__device__ __forceinline__ double shfl_xor(unsigned m, double v, int o, int w) { return __shfl_xor_sync(m, v, o, w); }
+__device__ __forceinline__ float shfl_xor(unsigned m, float v, int o, int w) { return __shfl_xor_sync(m, v, o, w); }
+__device__ __forceinline__ dfr shfl_xor(unsigned m, dfr v, int o, int w) {
+  return dfr{__shfl_xor_sync(m, v.h, o, w), __shfl_xor_sync(m, v.l, o, w)};
+}
+
+// accumulator of per-thread partial sums: FP64 for the native types, double-float for dfc
+template <typename V> struct acc_of { typedef double type; };
+template <> struct acc_of<dfc> { typedef dfr type; };
+template <typename A> __device__ __forceinline__ A to_acc(double v) { return from_double<A>(v); }
+template <typename A> __device__ __forceinline__ A to_acc(float v) { return (A)(double)v; }
+template <> __device__ __forceinline__ dfr to_acc<dfr>(float v) { return df_from_float(v); }
+template <typename A> __device__ __forceinline__ A to_acc(dfr v);
+template <> __device__ __forceinline__ dfr to_acc<dfr>(dfr v) { return v; }
 
 template <typename V>
 __device__ __forceinline__ V cmake(typename scalar_of<V>::type x, typename scalar_of<V>::type y) {
@@ -40,20 +81,40 @@ template <typename V> __device__ __forceinline__ V cscale(V a, typename scalar_o
   return cmake<V>(a.x * s, a.y * s);
 }
 
-// a * (-i) and a * (+i)
-template <typename V> __device__ __forceinline__ V cmul_mi(V a) { return cmake<V>(a.y, -a.x); }
-template <typename V> __device__ __forceinline__ V cmul_pi(V a) { return cmake<V>(-a.y, a.x); }
+template <> __device__ __forceinline__ dfc cadd<dfc>(dfc a, dfc b) { return dfc_add(a, b); }
+template <> __device__ __forceinline__ dfc csub<dfc>(dfc a, dfc b) { return dfc_sub(a, b); }
+template <> __device__ __forceinline__ dfc cmul<dfc>(dfc a, dfc b) { return dfc_mul(a, b); }
+template <> __device__ __forceinline__ dfc cmulc<dfc>(dfc a, dfc b) { return dfc_mulc(a, b); }
+template <> __device__ __forceinline__ dfc cscale<dfc>(dfc a, dfr s) { return dfc_scale(a, s); }
 
-// multiply by exp(-i*pi/4 * s) for the radix-8 inner twiddles:  (1 -+ i)/sqrt(2)
-template <typename V, bool FWD> __device__ __forceinline__ V cmul_w8_1(V a) {
-  typedef typename scalar_of<V>::type T;
-  const T h = T(0.70710678118654752440);
-  // FWD: a * (1 - i)/sqrt2 ; INV: a * (1 + i)/sqrt2
-  return FWD ? cmake<V>((a.x + a.y) * h, (a.y - a.x) * h) : cmake<V>((a.x - a.y) * h, (a.y + a.x) * h);
+// sign flips by a mask of the sign bit (0 or 0x80000000), on the integer pipe
+__device__ __forceinline__ float flip(float v, unsigned m) { return __int_as_float(__float_as_int(v) ^ (int)m); }
+__device__ __forceinline__ double flip(double v, unsigned m) {
+  return __hiloint2double(__double2hiint(v) ^ (int)m, __double2loint(v));
 }
-template <typename V, bool FWD> __device__ __forceinline__ V cmul_w8_3(V a) {
+__device__ __forceinline__ dfr flip(dfr v, unsigned m) { return dfr{flip(v.h, m), flip(v.l, m)}; }
+template <typename V> __device__ __forceinline__ V cflip(V a, unsigned m) { return cmake<V>(flip(a.x, m), flip(a.y, m)); }
+template <typename V> __device__ __forceinline__ V cconj_if(V a, unsigned m) { return cmake<V>(a.x, flip(a.y, m)); }
+
+// Transform direction of the FFT helpers: inv = 0 for the forward transform (exp(-i ...)),
+// 0x80000000 for the inverse; the direction is a run-time value so that one copy of the code
+// serves both.
+// a * (-i) forward, a * (+i) inverse
+template <typename V> __device__ __forceinline__ V cmul_mi_dir(V a, unsigned inv) {
+  return cmake<V>(flip(a.y, inv), flip(a.x, inv ^ 0x80000000u));
+}
+
+// 1/sqrt(2) in the working type (double-float: the FP32 pair nearest to it)
+template <typename T> __device__ __forceinline__ T rsqrt2() { return T(0.70710678118654752440); }
+template <> __device__ __forceinline__ dfr rsqrt2<dfr>() { return dfr{0.70710677f, 1.21016175e-08f}; }
+
+// a * exp(-+ i pi/4):  forward (x + y, y - x)/sqrt2, inverse (x - y, y + x)/sqrt2
+template <typename V> __device__ __forceinline__ V cmul_w8_1_dir(V a, unsigned inv) {
   typedef typename scalar_of<V>::type T;
-  const T h = T(0.70710678118654752440);
-  // FWD: a * (-1 - i)/sqrt2 ; INV: a * (-1 + i)/sqrt2
-  return FWD ? cmake<V>((a.y - a.x) * h, -(a.x + a.y) * h) : cmake<V>(-(a.x + a.y) * h, (a.x - a.y) * h);
+  const T h = rsqrt2<T>();
+  return cmake<V>((a.x + flip(a.y, inv)) * h, (a.y - flip(a.x, inv)) * h);
+}
+// a * exp(-+ 3 i pi/4) = (a * exp(-+ i pi/4)) * (-+ i)
+template <typename V> __device__ __forceinline__ V cmul_w8_3_dir(V a, unsigned inv) {
+  return cmul_mi_dir(cmul_w8_1_dir(a, inv), inv);
 }

@@ -8,7 +8,11 @@
 // Algorithm: the radix-R Stockham autosort FFT (Govindaraju et al., SC08,
 // "High Performance Discrete Fourier Transforms on Graphics Processors"),
 // mixed radix 8/4/2.  Twiddles come from a per-N table
-// tw[m] = exp(-2 pi i m / N) built on the host in extended precision.
+// tw[m] = exp(-2 pi i m / N) built on the host in extended precision; the
+// inverse transform uses their conjugates.  The direction is a run-time
+// argument so that a pass kernel holds one copy of the FFT code: the
+// double-float form of a 1024-point FFT alone is tens of kilobytes of
+// instructions, and several inlined copies overflow the instruction cache.
 //
 // Data placement.  Each thread owns E elements of the tile, all on one line:
 //   line = tid % LINES,  position p_k = tid / LINES + k * (N / E),  k = 0..E-1.
@@ -50,23 +54,23 @@ __device__ __forceinline__ void split_item(int u, int& line, int& b) {
 }
 
 // ---------------------------------------------------------------- radix kernels
-template <int R, bool FWD, typename V> struct Dft;
+// inv: 0 forward, 0x80000000 inverse (sign-bit mask, see aw_common.cuh)
+template <int R, typename V> struct Dft;
 
-template <bool FWD, typename V> struct Dft<2, FWD, V> {
-  __device__ __forceinline__ static void run(V* v) {
+template <typename V> struct Dft<2, V> {
+  __device__ __forceinline__ static void run(V* v, unsigned) {
     V a = v[0], b = v[1];
     v[0] = cadd(a, b);
     v[1] = csub(a, b);
   }
 };
 
-template <bool FWD, typename V> struct Dft<4, FWD, V> {
-  __device__ __forceinline__ static void run(V* v) {
+template <typename V> struct Dft<4, V> {
+  __device__ __forceinline__ static void run(V* v, unsigned inv) {
     V t0 = cadd(v[0], v[2]);
     V t1 = csub(v[0], v[2]);
     V t2 = cadd(v[1], v[3]);
-    V d = csub(v[1], v[3]);
-    V t3 = FWD ? cmul_mi(d) : cmul_pi(d);
+    V t3 = cmul_mi_dir(csub(v[1], v[3]), inv);
     v[0] = cadd(t0, t2);
     v[2] = csub(t0, t2);
     v[1] = cadd(t1, t3);
@@ -74,8 +78,8 @@ template <bool FWD, typename V> struct Dft<4, FWD, V> {
   }
 };
 
-template <bool FWD, typename V> struct Dft<8, FWD, V> {
-  __device__ __forceinline__ static void run(V* v) {
+template <typename V> struct Dft<8, V> {
+  __device__ __forceinline__ static void run(V* v, unsigned inv) {
     // y[2q]   = DFT4(a[n] + a[n+4])
     // y[2q+1] = DFT4((a[n] - a[n+4]) * w8^n)
     V b[4], c[4];
@@ -84,11 +88,11 @@ template <bool FWD, typename V> struct Dft<8, FWD, V> {
       b[n] = cadd(v[n], v[n + 4]);
       c[n] = csub(v[n], v[n + 4]);
     }
-    c[1] = cmul_w8_1<V, FWD>(c[1]);
-    c[2] = FWD ? cmul_mi(c[2]) : cmul_pi(c[2]);
-    c[3] = cmul_w8_3<V, FWD>(c[3]);
-    Dft<4, FWD, V>::run(b);
-    Dft<4, FWD, V>::run(c);
+    c[1] = cmul_w8_1_dir(c[1], inv);
+    c[2] = cmul_mi_dir(c[2], inv);
+    c[3] = cmul_w8_3_dir(c[3], inv);
+    Dft<4, V>::run(b, inv);
+    Dft<4, V>::run(c, inv);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       v[2 * q] = b[q];
@@ -103,8 +107,8 @@ template <int REM> struct RadixChoice {
 
 // Middle Stockham stage with span NS: shared memory to shared memory, in place
 // (all inputs are read before the barrier, all outputs written after it).
-template <class Tile, int NT, int NS, bool FWD, typename V>
-__device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __restrict__ tw, int tid) {
+template <class Tile, int NT, int NS, typename V>
+__device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __restrict__ tw, int tid, unsigned inv) {
   constexpr int N = Tile::N;
   constexpr int R = RadixChoice<N / NS>::R;
   constexpr int NB = N / R;
@@ -126,11 +130,8 @@ __device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __res
     split_item<Tile>(tid + m * NT, line, b);
     const int k = b & (NS - 1);
 #pragma unroll
-    for (int r = 1; r < R; ++r) {
-      V w = tw[r * k * (N / (NS * R))];
-      v[m][r] = FWD ? cmul(v[m][r], w) : cmulc(v[m][r], w);
-    }
-    Dft<R, FWD, V>::run(v[m]);
+    for (int r = 1; r < R; ++r) v[m][r] = cmul(v[m][r], cconj_if(tw[r * k * (N / (NS * R))], inv));
+    Dft<R, V>::run(v[m], inv);
     const int base = (b / NS) * NS * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) s[Tile::addr(line, base + r * NS)] = v[m][r];
@@ -138,13 +139,13 @@ __device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __res
   __syncthreads();
 }
 
-template <class Tile, int NT, int NS, bool FWD, typename V> struct MiddleStages {
+template <class Tile, int NT, int NS, typename V> struct MiddleStages {
   // applies stages NS, NS*R, ... up to but excluding the last one
-  __device__ __forceinline__ static void run(V* s, const V* tw, int tid) {
+  __device__ __forceinline__ static void run(V* s, const V* tw, int tid, unsigned inv) {
     constexpr int R = RadixChoice<Tile::N / NS>::R;
     if constexpr (NS * R < Tile::N) {
-      stockham_stage<Tile, NT, NS, FWD, V>(s, tw, tid);
-      MiddleStages<Tile, NT, NS * R, FWD, V>::run(s, tw, tid);
+      stockham_stage<Tile, NT, NS, V>(s, tw, tid, inv);
+      MiddleStages<Tile, NT, NS * R, V>::run(s, tw, tid, inv);
     }
   }
 };
@@ -157,10 +158,10 @@ template <int N> struct LastSpan<N, N> {
   static constexpr int value = N;
 };
 
-// Full FFT of every line of the tile, registers in and out.
+// Full FFT of every line of the tile, registers in and out; inv selects the direction.
 //   r[k] holds the thread's element at position tid / LINES + k * (N / E) of line tid % LINES.
-template <class Tile, int NT, bool FWD, typename V>
-__device__ __forceinline__ void tile_fft_regs(V* r, V* __restrict__ s, const V* __restrict__ tw, int tid) {
+template <class Tile, int NT, typename V>
+__device__ __forceinline__ void tile_fft_regs(V* r, V* __restrict__ s, const V* __restrict__ tw, int tid, unsigned inv) {
   constexpr int N = Tile::N;
   constexpr int L = Tile::LINES;
   constexpr int E = N * L / NT;
@@ -175,14 +176,14 @@ __device__ __forceinline__ void tile_fft_regs(V* r, V* __restrict__ s, const V* 
     V v[R1];
 #pragma unroll
     for (int q = 0; q < R1; ++q) v[q] = r[m + q * PER1];
-    Dft<R1, FWD, V>::run(v);
+    Dft<R1, V>::run(v, inv);
     int line, b;
     split_item<Tile>(tid + m * NT, line, b);
 #pragma unroll
     for (int q = 0; q < R1; ++q) s[Tile::addr(line, b * R1 + q)] = v[q];
   }
   __syncthreads();
-  MiddleStages<Tile, NT, R1, FWD, V>::run(s, tw, tid);
+  MiddleStages<Tile, NT, R1, V>::run(s, tw, tid, inv);
   // last stage: span NSL = N / RL; outputs land on the thread's own positions
   constexpr int NSL = LastSpan<N, R1>::value;
   constexpr int RL = N / NSL;
@@ -202,11 +203,8 @@ __device__ __forceinline__ void tile_fft_regs(V* r, V* __restrict__ s, const V* 
     split_item<Tile>(tid + m * NT, line, b);
     // b < NSL here, so the twiddle exponent is q * b and the outputs go to b + q * NSL
 #pragma unroll
-    for (int q = 1; q < RL; ++q) {
-      V w = tw[q * b];
-      v[m][q] = FWD ? cmul(v[m][q], w) : cmulc(v[m][q], w);
-    }
-    Dft<RL, FWD, V>::run(v[m]);
+    for (int q = 1; q < RL; ++q) v[m][q] = cmul(v[m][q], cconj_if(tw[q * b], inv));
+    Dft<RL, V>::run(v[m], inv);
 #pragma unroll
     for (int q = 0; q < RL; ++q) r[m + q * PERL] = v[m][q];
   }

@@ -71,6 +71,15 @@ template <> __device__ inline void aw_store<double>(void* aw_p, long long aw_k, 
 template <> __device__ inline void aw_store<cuda_complex>(void* aw_p, long long aw_k, int aw_f32, cuda_complex aw_v) {
   if (aw_f32) ((float2*)aw_p)[aw_k] = make_float2((float)aw_v._aw_re, (float)aw_v._aw_im);
   else ((double2*)aw_p)[aw_k] = make_double2(aw_v._aw_re, aw_v._aw_im); }
+// double-float form of a table entry (format 2): each FP64 number as the FP32 pair (hi, lo)
+__device__ inline float2 aw_df1(double aw_v) {
+  const float aw_h = (float)aw_v;
+  return make_float2(aw_h, (float)(aw_v - (double)aw_h));
+}
+__device__ inline float4 aw_df2(double aw_re, double aw_im) {
+  const float2 aw_a = aw_df1(aw_re), aw_b = aw_df1(aw_im);
+  return make_float4(aw_a.x, aw_a.y, aw_b.x, aw_b.y);
+}
 __device__ inline double2 aw_load(const void* aw_p, long long aw_k, int aw_f32) {
   if (aw_f32) { float2 aw_v = ((const float2*)aw_p)[aw_k]; return make_double2(aw_v.x, aw_v.y); }
   return ((const double2*)aw_p)[aw_k]; }
@@ -157,7 +166,8 @@ extern "C" __global__ void aw_tab(void* aw_col, void* aw_row, int aw_f32, int aw
     aw_im *= aw_f;
   }
   void* aw_dst = aw_c ? aw_col : aw_row;
-  if (aw_f32) ((float2*)aw_dst)[aw_idx] = make_float2((float)aw_re, (float)aw_im);
+  if (aw_f32 == 1) ((float2*)aw_dst)[aw_idx] = make_float2((float)aw_re, (float)aw_im);
+  else if (aw_f32 == 2) ((float4*)aw_dst)[aw_idx] = aw_df2(aw_re, aw_im);
   else ((double2*)aw_dst)[aw_idx] = make_double2(aw_re, aw_im);
 }
 
@@ -341,7 +351,8 @@ extern "C" __global__ void aw_mask2d(void* aw_out, int aw_f32, int aw_which, dou
   const double aw_v = aw_which == 0 ? aw_absx2d(i, j, XX, XX_prime, PP, PP_prime, t)
                                     : aw_absp2d(i, j, XX, XX_prime, PP, PP_prime, t);
   const long long aw_k = (long long)i * aw_ncol + j;
-  if (aw_f32) ((float*)aw_out)[aw_k] = (float)aw_v;
+  if (aw_f32 == 1) ((float*)aw_out)[aw_k] = (float)aw_v;
+  else if (aw_f32 == 2) ((float2*)aw_out)[aw_k] = aw_df1(aw_v);
   else ((double*)aw_out)[aw_k] = aw_v;
 }
 )AWSRC";

@@ -30,6 +30,7 @@ template <typename V, int N, int LINES> struct Shape {
 template <typename V> struct RealOf;
 template <> struct RealOf<double2> { typedef double type; };
 template <> struct RealOf<float2> { typedef float type; };
+template <> struct RealOf<dfc> { typedef dfr type; };
 
 // The thread's own elements (see aw_fft.cuh): line tid % LINES, positions pos0 + k * STEP.
 template <class Tile, int NT> struct Own {
@@ -58,46 +59,35 @@ __device__ __forceinline__ void apply_factor(V* r, const AwFactor& f, int lg, in
   if (ct) ct += tab_off;
   if (rt) rt += tab_off;
   if (mk) mk += elem_off;
-  T sc = (T)f.scale;
-  T sci = T(0);
+  double scr = f.scale, sci = 0.0;
   if (f.scale_ptr) {
-    sc = (T)(f.scale * f.scale_ptr[2 * inst]);
-    sci = (T)(f.scale * f.scale_ptr[2 * inst + 1]);
+    scr = f.scale * f.scale_ptr[2 * inst];
+    sci = f.scale * f.scale_ptr[2 * inst + 1];
   }
+  // every factor that depends only on the line, folded into one complex constant:
+  //   row tile: conj(row_tab[line]) * scale,  column tile: col_tab[line] * scale
+  V c = cmake<V>(from_double<T>(scr), from_double<T>(sci));
+  const V* lt = Tile::IS_ROW ? rt : ct;
+  if (lt) c = Tile::IS_ROW ? cmulc(c, lt[lg]) : cmul(c, lt[lg]);
+  const bool have_c = lt || scr != 1.0 || sci != 0.0;
+  const V* et = Tile::IS_ROW ? ct : rt;  // table along the line
   const int lo_n = f.sh_lo_n;
   const int nhi = lo_n ? Tile::N / lo_n : 0;
-  // factors that depend only on the line
-  V line_w = cmake<V>(T(1), T(0));
-  bool have_line_w = false;
-  if (Tile::IS_ROW && rt) {
-    line_w = rt[lg];
-    have_line_w = true;
-  }
-  if (!Tile::IS_ROW && ct) {
-    line_w = ct[lg];
-    have_line_w = true;
-  }
+  const int sgn = f.sign;
 #pragma unroll
   for (int k = 0; k < E; ++k) {
     const int pos = pos0 + k * STEP;
     const int i = Tile::IS_ROW ? lg : pos;
     const int j = Tile::IS_ROW ? pos : lg;
     V v = r[k];
-    T m = T(1);
-    if (f.sign && ((f.sign == 1 ? i + j : (f.sign == 2 ? i : j)) & 1)) m = -m;
+    if (sgn && ((sgn == 1 ? i + j : (sgn == 2 ? i : j)) & 1)) v = cflip(v, 0x80000000u);
     if (mk) {
       T q = mk[(long long)i * ncols + j];
-      m *= q;
-      if (f.mask_pow == 2) m *= q;
+      if (f.mask_pow == 2) q = q * q;
+      v = cscale(v, q);
     }
-    v = sci == T(0) ? cscale(v, m * sc) : cmul(v, cmake<V>(m * sc, m * sci));
-    if (Tile::IS_ROW) {
-      if (ct) v = cmul(v, ct[j]);
-      if (have_line_w) v = cmulc(v, line_w);
-    } else {
-      if (have_line_w) v = cmul(v, line_w);
-      if (rt) v = cmulc(v, rt[i]);
-    }
+    if (et) v = Tile::IS_ROW ? cmul(v, et[j]) : cmulc(v, et[i]);
+    if (have_c) v = cmul(v, c);
     if (lo_n) {
       const int q = (pos + f.sh_roll) & (Tile::N - 1);
       V w = cmul(sh[(long long)lg * nhi + q / lo_n], sl[(long long)lg * lo_n + (q % lo_n)]);
@@ -110,10 +100,7 @@ __device__ __forceinline__ void apply_factor(V* r, const AwFactor& f, int lg, in
 template <class Tile, int NT, typename V>
 __device__ __forceinline__ void run_fft(V* r, V* s, const V* tw, int dir, int tid) {
   if (dir == 0) return;
-  if (dir > 0)
-    tile_fft_regs<Tile, NT, true, V>(r, s, tw, tid);
-  else
-    tile_fft_regs<Tile, NT, false, V>(r, s, tw, tid);
+  tile_fft_regs<Tile, NT, V>(r, s, tw, tid, dir > 0 ? 0u : 0x80000000u);
 }
 
 template <typename V, class Tile, int NT>
@@ -124,7 +111,7 @@ __device__ __forceinline__ void store_regs(V* __restrict__ dst, const V* r, int 
   for (int k = 0; k < E; ++k) {
     const int pos = pos0 + k * STEP;
     V v = r[k];
-    if (sgn && ((lg + pos) & 1)) v = cmake<V>(-v.x, -v.y);
+    if (sgn && ((lg + pos) & 1)) v = cflip(v, 0x80000000u);
     dst[gidx<Tile>(lg, pos, ncols)] = v;
   }
 }
@@ -145,7 +132,7 @@ __device__ __forceinline__ double block_sum(double x, double* red, int tid) {
 }
 
 template <typename V, class Tile, int NT>
-__global__ void __launch_bounds__(NT) aw_pass_kernel(const AwPassArgs a) {
+__global__ void __launch_bounds__(NT) aw_pass_kernel(const __grid_constant__ AwPassArgs a) {
   extern __shared__ __align__(16) unsigned char aw_smem[];
   typedef typename RealOf<V>::type T;
   V* s = reinterpret_cast<V*>(aw_smem);
@@ -170,45 +157,54 @@ __global__ void __launch_bounds__(NT) aw_pass_kernel(const AwPassArgs a) {
 #pragma unroll
   for (int k = 0; k < E; ++k) r[k] = in[gidx<Tile>(lg, pos0 + k * STEP, ncols)];
 
-  if (a.f0.active) apply_factor<V, Tile, NT>(r, a.f0, lg, pos0, ncols, toff, eoff, inst);
-  run_fft<Tile, NT>(r, s, tw, a.d1, tid);
-  if (a.f1.active) apply_factor<V, Tile, NT>(r, a.f1, lg, pos0, ncols, toff, eoff, inst);
-
-  if (a.mid_out) store_regs<V, Tile, NT>((V*)a.mid_out + eoff, r, lg, pos0, ncols, a.mid_sign != 0);
-  if (Tile::IS_ROW && a.diag_out) {
+  // The pass as a loop over FFT segments, so that the kernel holds one copy of the FFT and of
+  // the factor code:
+  //   0: f0, FFT d1, f1        then mid_out, diag_out, red_abs2 (start)
+  //   1: keep, FFT br_d1, fbr  (branch, with br_out)
+  //   2: FFT br_d2, store br_out, restore
+  //   3: f2, FFT d2, f3
+  V keep[E];
+#pragma unroll 1
+  for (int seg = 0; seg < 4; ++seg) {
+    if ((seg == 1 || seg == 2) && !a.br_out) continue;
+    if (seg == 1) {
 #pragma unroll
-    for (int k = 0; k < E; ++k)
-      if (pos0 + k * STEP == lg)
-        a.diag_out[(long long)inst * a.nrows + lg] = make_double2((double)r[k].x, (double)r[k].y);
+      for (int k = 0; k < E; ++k) keep[k] = r[k];
+    }
+    const AwFactor* pre = seg == 0 ? &a.f0 : (seg == 3 ? &a.f2 : nullptr);
+    const AwFactor* post = seg == 0 ? &a.f1 : (seg == 1 ? &a.fbr : (seg == 3 ? &a.f3 : nullptr));
+    const int dir = seg == 0 ? a.d1 : (seg == 1 ? a.br_d1 : (seg == 2 ? a.br_d2 : a.d2));
+    if (pre && pre->active) apply_factor<V, Tile, NT>(r, *pre, lg, pos0, ncols, toff, eoff, inst);
+    run_fft<Tile, NT>(r, s, tw, dir, tid);
+    if (post && post->active) apply_factor<V, Tile, NT>(r, *post, lg, pos0, ncols, toff, eoff, inst);
+    if (seg == 0) {
+      if (a.mid_out) store_regs<V, Tile, NT>((V*)a.mid_out + eoff, r, lg, pos0, ncols, a.mid_sign != 0);
+      if (Tile::IS_ROW && a.diag_out) {
+#pragma unroll
+        for (int k = 0; k < E; ++k)
+          if (pos0 + k * STEP == lg)
+            a.diag_out[(long long)inst * a.nrows + lg] = make_double2(to_d(r[k].x), to_d(r[k].y));
+      }
+      if (Tile::IS_ROW && a.red_abs2 && !a.abs2_end) {
+        T acc = from_double<T>(0.0);
+#pragma unroll
+        for (int k = 0; k < E; ++k) acc += r[k].x * r[k].x + r[k].y * r[k].y;
+        const double tot = block_sum<NT>(to_d(acc), red, tid);
+        if (tid == 0) a.red_abs2[(long long)inst * gridDim.x + blockIdx.x] = tot;
+      }
+    }
+    if (seg == 2) {
+      store_regs<V, Tile, NT>((V*)a.br_out + eoff, r, lg, pos0, ncols, false);
+#pragma unroll
+      for (int k = 0; k < E; ++k) r[k] = keep[k];
+    }
   }
-  if (Tile::IS_ROW && a.red_abs2 && !a.abs2_end) {
-    T acc = T(0);
-#pragma unroll
-    for (int k = 0; k < E; ++k) acc += r[k].x * r[k].x + r[k].y * r[k].y;
-    const double tot = block_sum<NT>((double)acc, red, tid);
-    if (tid == 0) a.red_abs2[(long long)inst * gridDim.x + blockIdx.x] = tot;
-  }
-  if (a.br_out) {
-    V keep[E];
-#pragma unroll
-    for (int k = 0; k < E; ++k) keep[k] = r[k];
-    run_fft<Tile, NT>(r, s, tw, a.br_d1, tid);
-    if (a.fbr.active) apply_factor<V, Tile, NT>(r, a.fbr, lg, pos0, ncols, toff, eoff, inst);
-    run_fft<Tile, NT>(r, s, tw, a.br_d2, tid);
-    store_regs<V, Tile, NT>((V*)a.br_out + eoff, r, lg, pos0, ncols, false);
-#pragma unroll
-    for (int k = 0; k < E; ++k) r[k] = keep[k];
-  }
-
-  if (a.f2.active) apply_factor<V, Tile, NT>(r, a.f2, lg, pos0, ncols, toff, eoff, inst);
-  run_fft<Tile, NT>(r, s, tw, a.d2, tid);
-  if (a.f3.active) apply_factor<V, Tile, NT>(r, a.f3, lg, pos0, ncols, toff, eoff, inst);
   if (a.out) store_regs<V, Tile, NT>((V*)a.out + eoff, r, lg, pos0, ncols, false);
   if (Tile::IS_ROW && a.red_abs2 && a.abs2_end) {
-    T acc = T(0);
+    T acc = from_double<T>(0.0);
 #pragma unroll
     for (int k = 0; k < E; ++k) acc += r[k].x * r[k].x + r[k].y * r[k].y;
-    const double tot = block_sum<NT>((double)acc, red, tid);
+    const double tot = block_sum<NT>(to_d(acc), red, tid);
     if (tid == 0) a.red_abs2[(long long)inst * gridDim.x + blockIdx.x] = tot;
   }
 
@@ -218,7 +214,7 @@ __global__ void __launch_bounds__(NT) aw_pass_kernel(const AwPassArgs a) {
     // FP64 across threads in a fixed order
     if (a.col_alt || a.alt_cross) {
       __shared__ double2 cred[NT];
-      T cr = T(0), ci = T(0);
+      T cr = from_double<T>(0.0), ci = from_double<T>(0.0);
 #pragma unroll
       for (int k = 0; k < E; ++k) {
         const int pos = pos0 + k * STEP;
@@ -235,19 +231,19 @@ __global__ void __launch_bounds__(NT) aw_pass_kernel(const AwPassArgs a) {
           T xr = (lg & 1) ? -re : re, xi = (lg & 1) ? -im : im;
 #pragma unroll
           for (int o = B / 2; o > 0; o >>= 1) {
-            xr += __shfl_xor_sync(0xffffffffu, xr, o, B);
-            xi += __shfl_xor_sync(0xffffffffu, xi, o, B);
+            xr += shfl_xor(lane_mask<NT>(), xr, o, B);
+            xi += shfl_xor(lane_mask<NT>(), xi, o, B);
           }
           if (line == 0) {
             if (a.cluster > 1)
-              reinterpret_cast<double2*>(aw_smem + sizeof(V) * Tile::SMEM_ELEMS)[pos] = make_double2((double)xr, (double)xi);
+              reinterpret_cast<double2*>(aw_smem + sizeof(V) * Tile::SMEM_ELEMS)[pos] = make_double2(to_d(xr), to_d(xi));
             else
-              a.alt_cross[((long long)inst * gridDim.x + blockIdx.x) * a.nrows + pos] = make_double2((double)xr, (double)xi);
+              a.alt_cross[((long long)inst * gridDim.x + blockIdx.x) * a.nrows + pos] = make_double2(to_d(xr), to_d(xi));
           }
         }
       }
       if (a.col_alt) {
-        cred[tid] = make_double2((double)cr, (double)ci);
+        cred[tid] = make_double2(to_d(cr), to_d(ci));
         __syncthreads();
         if (tid < B) {
           double sr = 0.0, si = 0.0;
@@ -281,22 +277,23 @@ __global__ void __launch_bounds__(NT) aw_pass_kernel(const AwPassArgs a) {
       }
     }
     if (a.red_line || a.red_cross || a.red_sq) {
-      double lsum = 0.0, sq = 0.0;
+      typedef typename acc_of<V>::type A;
+      A lsum = to_acc<A>(0.0), sq = to_acc<A>(0.0);
 #pragma unroll
       for (int k = 0; k < E; ++k) {
         const int pos = pos0 + k * STEP;
-        const double re = (double)r[k].x, im = (double)r[k].y;
+        const A re = to_acc<A>(r[k].x), im = to_acc<A>(r[k].y);
         lsum += re;
         sq += re * re - im * im;
         if (a.red_cross) {
-          double c = re;
+          double c = to_d(re);
 #pragma unroll
-          for (int o = B / 2; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o, B);
+          for (int o = B / 2; o > 0; o >>= 1) c += __shfl_xor_sync(lane_mask<NT>(), c, o, B);
           if (line == 0) a.red_cross[((long long)inst * gridDim.x + blockIdx.x) * a.nrows + pos] = c;
         }
       }
       if (a.red_line) {
-        red[tid] = lsum;
+        red[tid] = to_d(lsum);
         __syncthreads();
         if (tid < B) {
           double acc = 0.0;
@@ -306,7 +303,7 @@ __global__ void __launch_bounds__(NT) aw_pass_kernel(const AwPassArgs a) {
         __syncthreads();
       }
       if (a.red_sq) {
-        const double tot = block_sum<NT>(sq, red, tid);
+        const double tot = block_sum<NT>(to_d(sq), red, tid);
         if (tid == 0) a.red_sq[(long long)inst * gridDim.x + blockIdx.x] = tot;
       }
     }
@@ -422,7 +419,17 @@ template <typename V, int N> static int launch_col_n(const AwPassArgs* a, int ba
   }
 }
 
-#define AW_FOR_SIZES(M) M(64) M(128) M(256) M(512) M(1024) M(2048) M(4096) M(8192)
+#define AW_FOR_SIZES(M) M(32) M(64) M(128) M(256) M(512) M(1024) M(2048) M(4096) M(8192)
+
+// Per-size launchers, so that the heavier element types can spread their instantiations over
+// several translation units that compile in parallel.
+#define AW_SIZE_LAUNCHERS(V, TAG, NN)                                                   \
+  int aw_##TAG##_row_##NN(const AwPassArgs* a, int batch, cudaStream_t st) {           \
+    return launch_row_n<V, NN>(a, batch, st);                                          \
+  }                                                                                    \
+  int aw_##TAG##_col_##NN(const AwPassArgs* a, int batch, cudaStream_t st) {           \
+    return launch_col_n<V, NN>(a, batch, st);                                          \
+  }
 
 template <typename V> static int launch_row(const AwPassArgs* a, int batch, cudaStream_t st) {
   switch (a->ncols) {

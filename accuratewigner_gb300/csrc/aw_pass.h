@@ -74,6 +74,8 @@ int aw_launch_row_pass_f64(const AwPassArgs* a, int batch, void* stream);
 int aw_launch_col_pass_f64(const AwPassArgs* a, int batch, void* stream);
 int aw_launch_row_pass_f32(const AwPassArgs* a, int batch, void* stream);
 int aw_launch_col_pass_f32(const AwPassArgs* a, int batch, void* stream);
+int aw_launch_row_pass_df(const AwPassArgs* a, int batch, void* stream);
+int aw_launch_col_pass_df(const AwPassArgs* a, int batch, void* stream);
 // number of column blocks (rows of red_cross) the column pass uses for a given N (single instance)
 int aw_col_pass_blocks(int nrows, int ncols, int f32);
 // columns per column-pass block for `batch` instances

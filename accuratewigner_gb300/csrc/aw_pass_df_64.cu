@@ -1,0 +1,4 @@
+// double-float pass kernels, line length 64
+#include "aw_pass.cuh"
+
+AW_SIZE_LAUNCHERS(dfc, df, 64)

@@ -10,18 +10,31 @@
 
 namespace {
 
+// element formats: 0 complex128, 1 complex64, 2 double-float complex (re hi, re lo, im hi, im lo)
 __device__ __forceinline__ double2 ld(const void* p, long long k, int f32) {
-  if (f32) {
+  if (f32 == 1) {
     float2 v = ((const float2*)p)[k];
     return make_double2(v.x, v.y);
   }
+  if (f32 == 2) {
+    float4 v = ((const float4*)p)[k];
+    return make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+  }
   return ((const double2*)p)[k];
 }
+__device__ __forceinline__ float2 df_split(double v) {
+  const float h = __double2float_rn(v);
+  return make_float2(h, __double2float_rn(v - (double)h));
+}
 __device__ __forceinline__ void st(void* p, long long k, int f32, double2 v) {
-  if (f32)
+  if (f32 == 1) {
     ((float2*)p)[k] = make_float2((float)v.x, (float)v.y);
-  else
+  } else if (f32 == 2) {
+    const float2 a = df_split(v.x), b = df_split(v.y);
+    ((float4*)p)[k] = make_float4(a.x, a.y, b.x, b.y);
+  } else {
     ((double2*)p)[k] = v;
+  }
 }
 
 __global__ void k_scale(void* a, int f32, long long n, double re, double im, const double* ptr) {

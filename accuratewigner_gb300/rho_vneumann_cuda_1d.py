@@ -22,7 +22,7 @@ class RhoVNeumannCUDA1D:
 
     Keywords (as rho_vneumann_cuda_1d.py:24-46): X_gridDIM, X_amplitude, V, K, dt, t, consts, functions,
     diff_V, diff_K, abs_boundary_x (function of X), abs_boundary_p (function of P).
-    Extra keyword: precision ('c128' default, or 'c64').
+    Extra keyword: precision ('c128' default, 'c128-fp64' or 'c64').
     """
 
     _kind = _lib.AW_RHO_VNEUMANN

@@ -22,7 +22,8 @@ class SchrodingerWignerCUDA1D:
     propagated wave function on demand, on one GB300.
 
     Keywords (as schrodinger_wigner_cuda_1d.py:28-48): X_gridDIM, X_amplitude, V, K, dt, t, consts, functions,
-    diff_V, diff_K, abs_boundary_x, abs_boundary_p.  Extra keyword: precision ('c128' default, or 'c64').
+    diff_V, diff_K, abs_boundary_x, abs_boundary_p.  Extra keyword: precision ('c128' default, or 'c64';
+    'c128' runs the one-dimensional passes in native FP64).
     """
 
     _kind = _lib.AW_SCHRODINGER

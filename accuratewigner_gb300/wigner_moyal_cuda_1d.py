@@ -22,7 +22,7 @@ class WignerMoyalCUDA1D:
 
     Keywords (as wigner_moyal_cuda_1d.py:19-41): X_gridDIM, X_amplitude, P_gridDIM, P_amplitude, V, K, dt,
     t (optional), consts, functions, diff_V, diff_K, abs_boundary_x, abs_boundary_p (optional).
-    Extra keywords of this implementation: precision ('c128' default, or 'c64'),
+    Extra keywords of this implementation: precision ('c128' default, 'c128-fp64' or 'c64'),
     extra_observables (tuple of strings recorded every step into self.extra_average).
     """
 

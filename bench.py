@@ -11,7 +11,7 @@ of the field-free Hamiltonian (synthetic: timing does not depend on it).
 A "step" is one split step including its per-step Wigner transform,
 normalisation and observables.  The metric is grid-point * steps / s.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision c128|c64]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision c128|c128-fp64|c64]
 """
 import argparse
 import ctypes
@@ -65,7 +65,9 @@ PARAMS = dict(
 INIT = "exp(-X * X - P * P) / M_PI"
 CHUNK = 50  # steps per propagate() call, as the reference's own driver loop (wigner_moyal_cuda_1d.py:954)
 
-STATE_BYTES_PER_PT = {"c128": 16, "c64": 8}
+STATE_BYTES_PER_PT = {"c128": 16, "c128-fp64": 16, "c64": 8}
+# arithmetic of the passes per precision
+DTYPE = {"c128": "c128 state, f32x2 double-float arithmetic", "c128-fp64": "f64", "c64": "f32+f64"}
 ALG_BYTES_FACTOR = 10  # bytes per grid point per step = 10 * S (propagation 4 S + per-step Wigner transform 6 S)
 
 
@@ -260,7 +262,7 @@ def run_ours(args):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64" if args.precision == "c128" else "f32+f64",
+            "dtype": DTYPE[args.precision],
             "data": "synthetic (config 2 shapes; Gibbs-state initial condition)",
             "config": {
                 "workload": "strong-field Wigner-Moyal, 1024x1024 (x,p), X_amplitude=60, P_amplitude=6, soft-core V + "
@@ -284,7 +286,8 @@ def run_ours(args):
                 "frac": (achieved / peak) if achieved else None,
                 "traffic": traffic,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s",
-                "note": "FP64 kernels are bound by the FP64 pipe, not HBM; frac is the HBM fraction of the dominant pass",
+                "note": "the passes are bound by arithmetic (FP64 pipe, or FP32 issue for double-float), not HBM; "
+                        "frac is the HBM fraction of the dominant pass",
             },
             "kernel_profile": prof,
             "clocks": clk.summary(),
@@ -370,7 +373,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="c128", choices=["c128", "c64"])
+    ap.add_argument("--precision", default="c128", choices=["c128", "c128-fp64", "c64"])
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

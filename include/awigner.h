@@ -40,8 +40,10 @@ extern "C" {
 #define AW_SCHRODINGER 4    /* SchrodingerWignerCUDA1D schrodinger_wigner_cuda_1d.py:16 */
 
 /* arithmetic of the state */
-#define AW_C128 0           /* complex128 throughout, as the reference (wigner_moyal_cuda_1d.py:629) */
+#define AW_C128 0           /* complex128 state, as the reference (wigner_moyal_cuda_1d.py:629); passes in
+                               double-float arithmetic (FP32 hi + lo pairs, about 2^-48 per operation) */
 #define AW_C64 1            /* complex64 butterflies and phases; FP64 tables and reductions */
+#define AW_C128_FP64 2      /* complex128 state, passes in native FP64 arithmetic */
 
 /* device buffers */
 #define AW_BUF_RHO 0        /* rho (WM/WB: Np x Nx in the rotated frame; VN/RB: N x N) */

@@ -28,6 +28,15 @@ def pytest_collection_modifyitems(config, items):
             item.add_marker(skip)
 
 
+@pytest.fixture(params=["c128", "c128-fp64"])
+def c128_engine(request, monkeypatch):
+    """Runs a complex128 parity test with both pass engines: double-float and native FP64."""
+    import accuratewigner_gb300._common as common
+
+    monkeypatch.setattr(common, "DEFAULT_PRECISION", request.param)
+    return request.param
+
+
 def rel_l2(a, b):
     import numpy as np
 

@@ -3,9 +3,9 @@ import pytest
 
 from golden_cases import CASES, compare, load_golden, run_ops
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("c128_engine")]
 
-TOL = 1e-10  # plain complex128 form
+TOL = 1e-10  # complex128 state, either pass engine
 
 
 def _gpu_cls(kind):

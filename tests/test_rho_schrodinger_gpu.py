@@ -4,7 +4,7 @@ import pytest
 
 from conftest import obs_close, rel_l2
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("c128_engine")]
 
 TOL = 1e-10
 

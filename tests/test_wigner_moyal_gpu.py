@@ -5,7 +5,7 @@ import pytest
 from conftest import obs_close, rel_l2
 from _cases import WM_ANHARMONIC, WM_INIT, WM_STRONG_FIELD, e_field
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("c128_engine")]
 
 TOL = 1e-10  # plain complex128 form: relative L2 against the FP64 oracle
 
