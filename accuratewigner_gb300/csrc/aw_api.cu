@@ -142,6 +142,9 @@ struct aw_state_s {
   int nr = 0, nc = 0;      // main grid rows x cols
   int wn = 0;              // Wigner grid side (VN: 2N; SW: N; WM: same as main)
   cudaStream_t st = nullptr;
+  // side stream of the per-step observable reduction of real-time propagation, and its events
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_z[2] = {nullptr, nullptr}, ev_f[2] = {nullptr, nullptr};
   cudaLibrary_t lib = nullptr;
   cudaKernel_t k_tab = nullptr, k_values = nullptr, k_final = nullptr, k_mask2d = nullptr;
   cudaKernel_t k_final_rot = nullptr;
@@ -151,6 +154,7 @@ struct aw_state_s {
   DevBuf tw_r, tw_c, tw_w;            // twiddles: row length (nc), column length (nr), Wigner grid (wn)
   DevBuf shx_hi, shx_lo, shy_hi, shy_lo;
   DevBuf tabs;                         // phase tables, slots of (nc + nr) complex
+  DevBuf vseq, vtimes;                 // time-dependent kick tables of a run of time points, their times
   DevBuf maskx, maskp;                 // 2-D masks (rotated frame)
   DevBuf red_line, red_cross, red_sq, rowsum, diag, abs2;
   DevBuf scal;                         // device scalars: [0..1] inv_norm (complex), [2..] misc
@@ -209,12 +213,22 @@ static void prof_clear(aw_state_s* h) {
   h->prof.clear();
 }
 
-static int hjit(aw_state_s* h, cudaKernel_t k, dim3 g, dim3 b, void** args) {
-  cudaEvent_t pe = prof_mark(h);
-  int r = jit_launch(k, g, b, args, h->st);
-  prof_done(h, PROF_JIT, 0.0, pe);
+static int hjit_on(aw_state_s* h, cudaKernel_t k, dim3 g, dim3 b, void** args, cudaStream_t st) {
+  cudaEvent_t pe = nullptr;
+  if (h->prof_on) {
+    cudaEventCreate(&pe);
+    cudaEventRecord(pe, st);
+  }
+  int r = jit_launch(k, g, b, args, st);
+  if (pe) {
+    cudaEvent_t pb;
+    cudaEventCreate(&pb);
+    cudaEventRecord(pb, st);
+    h->prof.push_back({PROF_JIT, 0.0, pe, pb});
+  }
   return r;
 }
+static int hjit(aw_state_s* h, cudaKernel_t k, dim3 g, dim3 b, void** args) { return hjit_on(h, k, g, b, args, h->st); }
 
 extern "C" int aw_profile(aw_handle h, int32_t enable) {
   if (!h) return fail(AW_E_ARG, "null handle");
@@ -481,9 +495,11 @@ enum { TAB_V1 = 0, TAB_V1B, TAB_V2, TAB_K, TAB_BV, TAB_BK, TAB_BLK, TAB_NSLOT };
 static void* tab_col(aw_state_s* h, int slot) { return (char*)h->tabs.p + (size_t)slot * (h->nc + h->nr) * h->esz; }
 static void* tab_row(aw_state_s* h, int slot) { return (char*)tab_col(h, slot) + (size_t)h->nc * h->esz; }
 
-// build one table slot: fn 0 = V, 1 = K
+// build one table slot: fn 0 = V, 1 = K.  With tlist (device times, count of them), builds count
+// tables of times tlist[s] + ta at col/row + s * (nc + nr) elements instead.
 static int build_tab(aw_state_s* h, int slot, int fn, int mode, double ta, double tb, double ca, double cb,
-                     double shift, int maskpow, double tmask) {
+                     double shift, int maskpow, double tmask, void* col_base = nullptr, const double* tlist = nullptr,
+                     int count = 1) {
   int ncol = h->nc, nrow = h->nr, roll = 0;
   double dcol, drow;
   const aw_config& c = h->cfg;
@@ -498,13 +514,14 @@ static int build_tab(aw_state_s* h, int slot, int fn, int mode, double ta, doubl
   } else {
     dcol = drow = fn == 0 ? c.dX : c.dP;
   }
-  void* col = tab_col(h, slot);
-  void* row = tab_row(h, slot);
+  void* col = col_base ? col_base : tab_col(h, slot);
+  void* row = (char*)col + (size_t)h->nc * h->esz;
   int f32 = tab_fmt(h);
+  long long tstride = (long long)h->nc + h->nr;
   void* args[] = {&col, &row, &f32, &fn, &mode, &ncol, &dcol, &roll, &nrow, &drow,
-                  &ta, &tb, &ca, &cb, &shift, &maskpow, &tmask};
+                  &ta, &tb, &ca, &cb, &shift, &maskpow, &tmask, &tlist, &tstride};
   const int n = ncol + nrow;
-  return hjit(h, h->k_tab, dim3((n + 31) / 32), dim3(32), args);
+  return hjit(h, h->k_tab, dim3((n + 31) / 32, count), dim3(32), args);
 }
 
 static int build_mask2d(aw_state_s* h, int which, double t) {
@@ -594,6 +611,13 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
     return fail(AW_E_ARG, "grid sides must be powers of two in [32, %d] (Wigner grid up to 8192)", maxn);
 
   CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+  if (h->kn.rotated) {
+    CK(cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+      CK(cudaEventCreateWithFlags(&h->ev_z[k], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&h->ev_f[k], cudaEventDisableTiming));
+    }
+  }
 
   // user module
   std::string src = awjit::module_source(h->kn, h->consts, h->V, h->K, h->absx, h->absp, h->obs_x, h->obs_p);
@@ -680,7 +704,7 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   TRY(dalloc(h->red_sq, (size_t)h->red_blocks * 8));
   TRY(dalloc(h->rowsum, (size_t)std::max(wr, wc) * 8));
   TRY(dalloc(h->diag, (size_t)std::max(h->nr, h->nc) * 16));
-  TRY(dalloc(h->abs2, (size_t)std::max(h->nr, 1) * 8));
+  TRY(dalloc(h->abs2, 2 * (size_t)std::max(h->nr, 1) * 8));  // two parities, see rot_run
   if (h->kn.rotated) {
     // the marginal column pass: narrow slabs spread over every SM, row partials summed across
     // clusters of 8 blocks in distributed shared memory, so that z_blocks stays small
@@ -688,8 +712,9 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
     const size_t z_smem = (size_t)h->nr * h->z_lines * h->esz + (size_t)h->nr * 16;
     h->z_cluster = (h->nc / h->z_lines) % 8 == 0 && h->nr % 8 == 0 && z_smem <= 160 * 1024 ? 8 : 1;
     h->z_blocks = h->nc / h->z_lines / h->z_cluster;
-    TRY(dalloc(h->zbuf, (size_t)(h->nc + h->nr) * 16));
-    TRY(dalloc(h->altbuf, (size_t)h->z_blocks * h->nr * 16));
+    // two parities, so that step n's reduction can run while step n + 1 writes the other
+    TRY(dalloc(h->zbuf, 2 * (size_t)(h->nc + h->nr) * 16));
+    TRY(dalloc(h->altbuf, 2 * (size_t)h->z_blocks * h->nr * 16));
   }
 
   // 2-D absorbing masks of the rotated frame
@@ -758,13 +783,22 @@ extern "C" int aw_create(const aw_config* cfg, aw_handle* out) {
 extern "C" int aw_destroy(aw_handle h) {
   if (!h) return AW_OK;
   if (h->st) cudaStreamSynchronize(h->st);
-  DevBuf* bufs[] = {&h->zbuf, &h->altbuf, &h->twist_hi, &h->twist_lo, &h->rho, &h->W, &h->snap, &h->tmp, &h->stage, &h->tw_r, &h->tw_c, &h->tw_w, &h->shx_hi,
+  DevBuf* bufs[] = {&h->vseq, &h->vtimes, &h->zbuf, &h->altbuf, &h->twist_hi, &h->twist_lo, &h->rho, &h->W, &h->snap, &h->tmp, &h->stage, &h->tw_r, &h->tw_c, &h->tw_w, &h->shx_hi,
                     &h->shx_lo, &h->shy_hi, &h->shy_lo, &h->tabs, &h->maskx, &h->maskp, &h->red_line,
                     &h->red_cross, &h->red_sq, &h->rowsum, &h->diag, &h->abs2, &h->scal, &h->stop, &h->hist,
                     &h->terms, &h->part, &h->blk_tabs};
   for (DevBuf* b : bufs) dfree(*b);
   for (DevBuf& b : h->sw_states) dfree(b);
   if (h->st) cudaStreamDestroy(h->st);
+  if (h->st2) {
+    cudaStreamSynchronize(h->st2);
+    cudaStreamDestroy(h->st2);
+  }
+  for (int k = 0; k < 2; ++k) {
+    if (h->ev_z[k]) cudaEventDestroy(h->ev_z[k]);
+    if (h->ev_f[k]) cudaEventDestroy(h->ev_f[k]);
+  }
+  prof_clear(h);
   delete h;
   return AW_OK;
 }
@@ -1107,11 +1141,17 @@ static int launch_finalize(aw_state_s* h, double t, double* hist_row, int stop_o
   return launch_finalize_args(h, f, t, hist_row, stop_on_purity);
 }
 
-static int launch_finalize_rot(aw_state_s* h, double t, double* hist_row, int stop_on_purity) {
-  const double2* z = (const double2*)h->zbuf.p;
-  const double2* wpart = (const double2*)h->altbuf.p;
+// marginal buffers of parity par (zbuf, altbuf, abs2 hold two sets)
+static double2* zbuf_of(aw_state_s* h, int par) { return (double2*)h->zbuf.p + (size_t)par * (h->nc + h->nr); }
+static double2* altbuf_of(aw_state_s* h, int par) { return (double2*)h->altbuf.p + (size_t)par * h->z_blocks * h->nr; }
+static double* abs2_of(aw_state_s* h, int par) { return (double*)h->abs2.p + (size_t)par * std::max(h->nr, 1); }
+
+static int launch_finalize_rot(aw_state_s* h, double t, double* hist_row, int stop_on_purity, int par = 0,
+                               cudaStream_t st = nullptr) {
+  const double2* z = zbuf_of(h, par);
+  const double2* wpart = altbuf_of(h, par);
   int nparts = h->z_blocks;
-  const double* abs2 = (const double*)h->abs2.p;
+  const double* abs2 = abs2_of(h, par);
   int nb2 = aw_row_pass_blocks(h->nr, h->nc, h->f32);
   double* tv = dscal(h, 16);
   unsigned int* counter = (unsigned int*)h->stop.p + 1;
@@ -1129,7 +1169,7 @@ static int launch_finalize_rot(aw_state_s* h, double t, double* hist_row, int st
   while (nchunk > 1 && ((std::min(ncol, nrow) % nchunk) || (nterms + 2) * nchunk > 1024)) nchunk >>= 1;
   void* args[] = {&z, &wpart, &nparts, &abs2, &nb2, &tv, &counter, &hist_row, &inv, &stop, &stop_on_purity, &t,
                   &ncol, &nrow, &dX, &dP, &dXdP, &ts, &tk, &ti, &tc, &nterms, &nslots, &nchunk};
-  return hjit(h, h->k_final_rot, dim3((nterms + 2) * nchunk), dim3(128), args);
+  return hjit_on(h, h->k_final_rot, dim3((nterms + 2) * nchunk), dim3(128), args, st ? st : h->st);
 }
 
 static int ensure_hist(aw_state_s* h, long long rows) {
@@ -1253,33 +1293,60 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
   const bool kdep = !p.bloch && (c.k_time_dependent || c.absp_mode == 2);
   const long long grid = (long long)h->nr * h->nc;
   const double inv_n2 = p.bloch ? 1.0 : 1.0 / (double)grid;  // WM divides by N^2 (wm:557); Bloch does not
-  // scale applied in the column pass: 1/N^2 and, with per-step normalisation, 1/norm of the previous step
+  // Real-time propagation is linear and every recorded observable is a ratio to the norm of the
+  // same step (sum f W / sum W, purity sum W^2 / (sum W)^2), so the per-step normalisation of
+  // normalize_rho_wigner (wm:608-622) is deferred to the end of the call: the step loop does not
+  // wait for the reduction, which runs on a side stream.  Bloch steps normalise every step.
+  const bool defer = !p.bloch && p.ehrenfest && h->st2;
+  // scale applied in the column pass: 1/N^2 and, for Bloch steps, 1/norm of the previous step
   KL(aw_k_set2(dscal(h, 0), 1.0, 0.0, h->st));
-  if (p.stop_on_purity) CK(cudaMemsetAsync(h->stop.p, 0, sizeof(int), h->st));
+  CK(cudaMemsetAsync(h->stop.p, 0, sizeof(int), h->st));  // a stop raised by an earlier call must not persist
   const int* stop = p.stop_on_purity ? (const int*)h->stop.p : nullptr;
 
   if (!vdep) TRY(rot_tables_V(h, p, times[1], times[1], false));
   if (!kdep) TRY(rot_tables_K(h, p, times[1]));
-  // with a time-dependent V the kick tables alternate between two slots, so that each time
-  // point's table is built once: slot of step n holds exp(-i dt/2 V(., t_n + dt/2))
-  auto vslot = [&](long long n) { return (!vdep || (n & 1)) ? TAB_V1 : TAB_V1B; };
-  auto vbuild = [&](long long n) -> int {
-    const double half = 0.5 * c.dt;
-    return build_tab(h, vslot(n), 0, 0, times[n] + half, 0.0, -half, 0.0, 0.0, 0, 0.0);
+  // With a time-dependent V the kick tables of up to VSEQ consecutive time points are built by one
+  // launch: table s of the run holds exp(-i dt/2 V(., t_{n0+s} + dt/2)).
+  const long long VSEQ = 256;
+  long long vs_n0 = 0, vs_cnt = 0;
+  if (vdep) {
+    TRY(dalloc(h->vseq, (size_t)VSEQ * (h->nc + h->nr) * h->esz));
+    TRY(dalloc(h->vtimes, (size_t)VSEQ * sizeof(double)));
+  }
+  // kick factor of time point n (table slot TAB_V1 when V does not depend on time)
+  auto vfactor = [&](long long n, bool sign, AwFactor* f) -> int {
+    TRY(vkick(h, p, TAB_V1, sign, times[n], f));
+    if (!vdep) return AW_OK;
+    const long long need_hi = std::min(n + 1, steps + 1);
+    if (n < vs_n0 || need_hi >= vs_n0 + vs_cnt) {
+      vs_n0 = n;
+      vs_cnt = std::min(VSEQ, steps + 2 - n);
+      std::vector<double> tl(times.begin() + n, times.begin() + n + vs_cnt);
+      // from pageable memory: staged before the call returns, ordered on the stream
+      CK(cudaMemcpyAsync(h->vtimes.p, tl.data(), tl.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
+      const double half = 0.5 * c.dt;
+      TRY(build_tab(h, 0, 0, 0, half, 0.0, -half, 0.0, 0.0, 0, 0.0, h->vseq.p, (const double*)h->vtimes.p,
+                    (int)vs_cnt));
+    }
+    f->col_tab = (char*)h->vseq.p + (size_t)(n - vs_n0) * (h->nc + h->nr) * h->esz;
+    f->row_tab = (char*)f->col_tab + (size_t)h->nc * h->esz;
+    return AW_OK;
   };
 
   // first kick: rho (position) -> S V(t_1) -> fft1
   {
-    if (vdep) TRY(vbuild(1));
     AwPassArgs a = pnone(h);
     a.in = a.out = h->rho.p;
-    TRY(vkick(h, p, vslot(1), true, times[1], &a.f2));
+    TRY(vfactor(1, true, &a.f2));
     a.d2 = +1;
     a.stop = stop;
     TRY(row_pass(h, a, h->tw_r));
   }
   for (long long n = 1; n <= steps; ++n) {
     const bool last = n == steps;
+    const int par = defer ? (int)(n & 1) : 0;
+    // the reduction of step n - 2 read this parity's buffers
+    if (defer && n >= 3) CK(cudaStreamWaitEvent(h->st, h->ev_f[par], 0));
     // column pass: scale, ifft0, K-kick, fft0
     {
       if (kdep) TRY(rot_tables_K(h, p, times[n]));
@@ -1287,7 +1354,7 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       a.in = a.out = h->rho.p;
       a.f0 = fnone();
       a.f0.scale = inv_n2;
-      a.f0.scale_ptr = p.ehrenfest ? dscal(h, 0) : nullptr;
+      a.f0.scale_ptr = p.ehrenfest && !defer ? dscal(h, 0) : nullptr;
       a.f0.active = 1;
       a.d1 = -1;
       a.f1 = ftab(h, p.bloch ? TAB_BK : TAB_K);
@@ -1305,24 +1372,23 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
     }
     // row pass: ifft1, V-kick(t_n) [branch: Wigner transform] [next kick(t_{n+1}), fft1 | S]
     {
-      if (vdep && !last) TRY(vbuild(n + 1));
       AwPassArgs a = pnone(h);
       a.in = a.out = h->rho.p;
       a.d1 = -1;
-      TRY(vkick(h, p, vslot(n), false, times[n], &a.f1));
+      TRY(vfactor(n, false, &a.f1));
       if (p.ehrenfest) {
         a.br_out = h->W.p;
         a.br_d1 = +1;
         a.fbr = fshear_x(h);
         a.br_d2 = -1;
-        a.red_abs2 = (double*)h->abs2.p;  // Sum |rho_n|^2 for the purity
+        a.red_abs2 = abs2_of(h, par);  // Sum |rho_n|^2 for the purity
       }
       if (p.keep_rho) {
         a.mid_out = h->snap.p;
         a.mid_sign = 1;
       }
       if (!last) {
-        TRY(vkick(h, p, vslot(n + 1), false, times[n + 1], &a.f2));
+        TRY(vfactor(n + 1, false, &a.f2));
         a.d2 = +1;
       } else {
         a.f2 = fsign();
@@ -1339,19 +1405,29 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       a.in = h->W.p;
       a.d1 = +1;
       a.f1 = fshear_y(h);
-      a.col_alt = (double2*)h->zbuf.p;
-      a.alt_cross = (double2*)h->altbuf.p;
+      a.col_alt = zbuf_of(h, par);
+      a.alt_cross = altbuf_of(h, par);
       a.lines_hint = h->z_lines;
       a.cluster = h->z_cluster;
       a.stop = stop;
       TRY(col_pass(h, a, h->tw_c));
-      TRY(launch_finalize_rot(h, times[n], hist + (size_t)(n - 1) * h->hist_cols, p.stop_on_purity));
+      double* hrow = hist + (size_t)(n - 1) * h->hist_cols;
+      if (defer) {
+        CK(cudaEventRecord(h->ev_z[par], h->st));
+        CK(cudaStreamWaitEvent(h->st2, h->ev_z[par], 0));
+        TRY(launch_finalize_rot(h, times[n], hrow, 0, par, h->st2));
+        CK(cudaEventRecord(h->ev_f[par], h->st2));
+      } else {
+        TRY(launch_finalize_rot(h, times[n], hrow, p.stop_on_purity));
+      }
       if (last) {
         WignerGrid g{h->W.p, h->nr, h->nc, &h->tw_r, &h->tw_c};
         TRY(wigner_passes(h, g, h->W.p, fnone(), false, false, true, true));
       }
     }
   }
+  // join: the last reduction wrote the history and 1/norm that the caller applies
+  if (defer && steps > 0) CK(cudaStreamWaitEvent(h->st, h->ev_f[(int)(steps & 1)], 0));
   return AW_OK;
 }
 
@@ -1556,7 +1632,7 @@ static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::ve
   const bool kdep = !p.bloch && c.k_time_dependent;
   const int N = h->nc;
   KL(aw_k_set2(dscal(h, 0), 1.0, 0.0, h->st));
-  if (p.stop_on_purity) CK(cudaMemsetAsync(h->stop.p, 0, sizeof(int), h->st));
+  CK(cudaMemsetAsync(h->stop.p, 0, sizeof(int), h->st));  // a stop raised by an earlier call must not persist
   const int* stop = p.stop_on_purity ? (const int*)h->stop.p : nullptr;
   const int row_blocks = aw_row_pass_blocks(h->nr, h->nc, h->f32);
   const int vslot = p.bloch ? TAB_BV : TAB_V1;

@@ -139,12 +139,21 @@ inline std::string module_source(const KindNames& kn, const std::string& consts,
 // x_i = aw_drow (i - aw_nrow/2).  aw_mode 0: exp(i (ca F(x,ta) + cb F(x,tb)));
 // aw_mode 1: exp(ca (F(x,ta) - shift)) (real).  F = V (aw_fn 0) or K (aw_fn 1).
 // aw_maskpow > 0 multiplies by the one-dimensional absorbing boundary.
+// With aw_tlist, blockIdx.y = s builds the tables of time aw_tlist[s] + aw_ta at
+// aw_col / aw_row + s * aw_tstride elements (one launch for a run of time points).
 extern "C" __global__ void aw_tab(void* aw_col, void* aw_row, int aw_f32, int aw_fn, int aw_mode,
                                   int aw_ncol, double aw_dcol, int aw_roll, int aw_nrow, double aw_drow,
                                   double aw_ta, double aw_tb, double aw_ca, double aw_cb, double aw_shift,
-                                  int aw_maskpow, double aw_tmask) {
+                                  int aw_maskpow, double aw_tmask, const double* aw_tlist, long long aw_tstride) {
   const int aw_k = blockIdx.x * blockDim.x + threadIdx.x;
   if (aw_k >= aw_ncol + aw_nrow) return;
+  if (aw_tlist) {
+    const int aw_s = blockIdx.y;
+    aw_ta += aw_tlist[aw_s];
+    const long long aw_off = aw_s * aw_tstride * (aw_f32 == 1 ? 8 : 16);
+    aw_col = (char*)aw_col + aw_off;
+    aw_row = (char*)aw_row + aw_off;
+  }
   const bool aw_c = aw_k < aw_ncol;
   const int aw_n = aw_c ? aw_ncol : aw_nrow;
   const int aw_idx = aw_c ? aw_k : aw_k - aw_ncol;
