@@ -187,6 +187,26 @@ def mask_mode(info, expr):
     return 2 if info.depends_on(expr, "t") else 1
 
 
+def apply_batch(cfg, kwargs, keep):
+    """Batch fields of an AwConfig from the keywords n_inst, batch_params, batch_init.
+
+    n_inst instances of the propagator share the handle; batch_params are the names of the
+    per-instance constants (usable in V, K, the absorbing boundaries, the observables and
+    batch_init, the initial state of an instance).  No reference counterpart: the batched
+    and served forms.
+    """
+    names = [str(n) for n in kwargs.get("batch_params", ()) or ()]
+    cfg.n_inst = int(kwargs.get("n_inst", 1) or 1)
+    cfg.n_params = len(names)
+    arr = (ctypes.c_char_p * max(1, len(names)))(*[n.encode() for n in names])
+    keep.append(arr)
+    cfg.param_names = arr
+    init = kwargs.get("batch_init", "") or ""
+    b = init.encode()
+    keep.append(b)
+    cfg.init_expr = b
+
+
 class Handle:
     """Owns one native propagator handle."""
 

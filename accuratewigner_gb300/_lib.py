@@ -79,6 +79,10 @@ class AwConfig(ctypes.Structure):
         ("term_coef", ctypes.POINTER(c_dbl)),
         ("n_slots", c_int),
         ("obs_p_time_dependent", c_int),
+        ("n_inst", c_int),
+        ("n_params", c_int),
+        ("param_names", ctypes.POINTER(c_cp)),
+        ("init_expr", c_cp),
     ]
 
 
@@ -120,6 +124,13 @@ SIGNATURES = [
     ("aw_sw_get_state", c_int, [c_vp, c_int, c_vp]),
     ("aw_sw_energy", c_int, [c_vp, c_dbl, ctypes.POINTER(c_dbl)]),
     ("aw_reduce_noalloc", c_int, [c_vp, c_int, c_i64, c_i64, c_int, c_vp, c_vp]),
+    ("aw_set_view", c_int, [c_vp, c_int, c_int]),
+    ("aw_set_params", c_int, [c_vp, c_int, ctypes.POINTER(c_dbl)]),
+    ("aw_set_active", c_int, [c_vp, ctypes.POINTER(c_int)]),
+    ("aw_init_state", c_int, [c_vp]),
+    ("aw_history_of", c_int, [c_vp, c_int, c_vp, c_i64, ctypes.POINTER(c_i64), ctypes.POINTER(c_int)]),
+    ("aw_gibbs_batch", c_int, [c_vp, ctypes.POINTER(c_dbl), c_i64, ctypes.POINTER(c_i64), ctypes.POINTER(c_dbl)]),
+    ("aw_bloch_min_of", c_int, [c_vp, c_int, ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl)]),
 ]
 
 _lib = None

@@ -137,6 +137,19 @@ struct aw_state_s {
   awjit::KindNames kn;
   int kind = 0, f32 = 0, esz = 16;
   int df = 0;                          // complex128 state, passes in double-float arithmetic
+  // batches: ni instances (1 for a single propagator), np parameters each; calls act on the
+  // view [v0, v0 + vc) and the step loops advance its active instances
+  int ni = 1, np = 0, v0 = 0, vc = 1;
+  std::vector<std::string> pnames;
+  std::string init_expr;
+  DevBuf params;                       // ni x np, row-major
+  DevBuf bvec;                         // Bloch coefficients per instance: ca_V, shift_V, ca_K, shift_K (4 x ni)
+  std::vector<int> active;             // per instance
+  std::vector<double> vmin_i, kmin_i;  // Bloch minima per instance
+  std::vector<char> minima_ok;
+  int col_lines = 0;                   // columns per column-pass block of a batch (fixed, so that an
+                                       // instance computes the same way whatever the view)
+  cudaKernel_t k_binit = nullptr;
   // buffers currently holding double-float state (pointer, elements); plain complex128 at rest
   std::vector<std::pair<void*, long long>> df_live;
   int nr = 0, nc = 0;      // main grid rows x cols
@@ -213,6 +226,30 @@ static void prof_clear(aw_state_s* h) {
   h->prof.clear();
 }
 
+// device scalars: [0, 2 ni) 1/norm of each instance (complex), then 16 spare, then the
+// finalize partials of each instance (FIN_TV doubles apiece)
+static constexpr int FIN_TV = 1088;
+static double* dinv(aw_state_s* h, int inst = 0) { return (double*)h->scal.p + 2 * inst; }
+static double* dmisc(aw_state_s* h, int k) { return (double*)h->scal.p + 2 * h->ni + k; }
+static double* dtv(aw_state_s* h, int inst) { return (double*)h->scal.p + 2 * h->ni + 16 + (size_t)inst * FIN_TV; }
+// per-instance stop flags and finalize counters
+static int* dstop(aw_state_s* h, int inst = 0) { return (int*)h->stop.p + inst; }
+static unsigned int* dcounter(aw_state_s* h, int inst) { return (unsigned int*)h->stop.p + h->ni + inst; }
+static long long gsz(const aw_state_s* h) { return (long long)h->nr * h->nc; }
+static void* at_inst(void* base, long long elems, int esz, int inst) {
+  return base ? (char*)base + (size_t)inst * elems * esz : nullptr;
+}
+// scale every instance of the view of `buf` (elems per instance) by its 1/norm
+static int vscale(aw_state_s* h, void* buf, long long elems) {
+  KL(aw_k_scale_n(at_inst(buf, elems, h->esz, h->v0), h->f32, elems, h->vc, 1.0, 0.0, dinv(h, h->v0), h->st));
+  return AW_OK;
+}
+// reset 1/norm of every instance of the view to 1
+static int vinv_reset(aw_state_s* h) {
+  KL(aw_k_fill(dinv(h, h->v0), 0, h->vc, 1.0, 0.0, h->st));
+  return AW_OK;
+}
+
 static int hjit_on(aw_state_s* h, cudaKernel_t k, dim3 g, dim3 b, void** args, cudaStream_t st) {
   cudaEvent_t pe = nullptr;
   if (h->prof_on) {
@@ -276,6 +313,7 @@ static int dalloc(DevBuf& b, size_t bytes) {
 }
 
 static bool is_pow2(long long n) { return n >= 2 && (n & (n - 1)) == 0; }
+
 
 static double define_round(double v) {
   // the value a kernel sees after '#define name %.15e' (wigner_moyal_cuda_1d.py:176)
@@ -404,12 +442,19 @@ static AwFactor fsign() {
   f.active = 1;
   return f;
 }
+// phase table slots (a batch holds one set per instance)
+enum { TAB_V1 = 0, TAB_V1B, TAB_V2, TAB_K, TAB_BV, TAB_BK, TAB_BLK, TAB_NSLOT };
+
+// a pass over the main grid of every instance of the view
 static AwPassArgs pnone(const aw_state_s* h) {
   AwPassArgs a;
   memset(&a, 0, sizeof a);
   a.f0 = a.f1 = a.f2 = a.f3 = a.fbr = fnone();
   a.nrows = h->nr;
   a.ncols = h->nc;
+  a.batch_elems = (long long)h->nr * h->nc;
+  a.batch_tab = (long long)TAB_NSLOT * (h->nc + h->nr);
+  a.inst0 = h->v0;
   return a;
 }
 
@@ -451,55 +496,68 @@ struct Settled {
   }
 };
 
-static int df_prepare(aw_state_s* h, AwPassArgs& a) {
-  const long long n = (long long)a.nrows * a.ncols;
-  if (a.in && !df_is_live(h, a.in)) {
-    void* dst = a.out ? a.out : (void*)a.in;
-    KL(aw_k_convert(a.in, 0, dst, 2, n, h->st));
-    a.in = dst;
+// the part of a state buffer a pass touches: the instances [inst0, inst0 + batch) of the view
+static void* df_region(const AwPassArgs& a, const void* base) {
+  return base ? (char*)base + (size_t)a.inst0 * a.batch_elems * 16 : nullptr;
+}
+static int df_prepare(aw_state_s* h, AwPassArgs& a, int batch) {
+  const long long n = (long long)batch * a.batch_elems;
+  void* rin = df_region(a, a.in);
+  if (rin && !df_is_live(h, rin)) {
+    void* base = a.out ? a.out : (void*)a.in;
+    void* dst = df_region(a, base);
+    KL(aw_k_convert(rin, 0, dst, 2, n, h->st));
+    a.in = base;
     df_mark(h, dst, n);
   }
   return AW_OK;
 }
-static void df_outputs(aw_state_s* h, const AwPassArgs& a) {
-  const long long n = (long long)a.nrows * a.ncols;
-  df_mark(h, a.out, n);
-  df_mark(h, a.mid_out, n);
-  df_mark(h, a.br_out, n);
+static void df_outputs(aw_state_s* h, const AwPassArgs& a, int batch) {
+  const long long n = (long long)batch * a.batch_elems;
+  df_mark(h, df_region(a, a.out), n);
+  df_mark(h, df_region(a, a.mid_out), n);
+  df_mark(h, df_region(a, a.br_out), n);
 }
 
 static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row) {
   a.tw = tw.p;
-  if (h->df) TRY(df_prepare(h, a));
+  const int batch = h->vc;
+  if (h->ni > 1) {
+    // every pass of a batch skips the instances that are stopped or inactive, and splits its
+    // columns the same way whatever the view
+    if (!a.stop) a.stop = dstop(h);
+    if (!row && !a.lines_hint) a.lines_hint = h->col_lines;
+  }
+  if (h->df) TRY(df_prepare(h, a, batch));
   cudaEvent_t pe = prof_mark(h);
   int r;
   if (h->df)
-    r = row ? aw_launch_row_pass_df(&a, 1, h->st) : aw_launch_col_pass_df(&a, 1, h->st);
+    r = row ? aw_launch_row_pass_df(&a, batch, h->st) : aw_launch_col_pass_df(&a, batch, h->st);
   else if (h->f32)
-    r = row ? aw_launch_row_pass_f32(&a, 1, h->st) : aw_launch_col_pass_f32(&a, 1, h->st);
+    r = row ? aw_launch_row_pass_f32(&a, batch, h->st) : aw_launch_col_pass_f32(&a, batch, h->st);
   else
-    r = row ? aw_launch_row_pass_f64(&a, 1, h->st) : aw_launch_col_pass_f64(&a, 1, h->st);
-  prof_done(h, row ? PROF_ROW : PROF_COL, pass_bytes(h, a), pe);
+    r = row ? aw_launch_row_pass_f64(&a, batch, h->st) : aw_launch_col_pass_f64(&a, batch, h->st);
+  prof_done(h, row ? PROF_ROW : PROF_COL, pass_bytes(h, a) * batch, pe);
   ++g_launches;
   if (r)
     return fail(AW_E_CUDA, "%s pass launch failed (%d, %s), grid %d x %d", row ? "row" : "column", r,
                 cudaGetErrorString(cudaGetLastError()), a.nrows, a.ncols);
-  if (h->df) df_outputs(h, a);
+  if (h->df) df_outputs(h, a, batch);
   return AW_OK;
 }
 static int row_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw) { return launch_pass(h, a, tw, true); }
 static int col_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw) { return launch_pass(h, a, tw, false); }
 
-// phase table slots
-enum { TAB_V1 = 0, TAB_V1B, TAB_V2, TAB_K, TAB_BV, TAB_BK, TAB_BLK, TAB_NSLOT };
 static void* tab_col(aw_state_s* h, int slot) { return (char*)h->tabs.p + (size_t)slot * (h->nc + h->nr) * h->esz; }
 static void* tab_row(aw_state_s* h, int slot) { return (char*)tab_col(h, slot) + (size_t)h->nc * h->esz; }
 
 // build one table slot: fn 0 = V, 1 = K.  With tlist (device times, count of them), builds count
 // tables of times tlist[s] + ta at col/row + s * (nc + nr) elements instead.
+// For a batch, the slot's tables of every instance of the view are built, each with its own
+// parameters and, given ca_vec / shift_vec (device, one per instance), its own ca and shift.
 static int build_tab(aw_state_s* h, int slot, int fn, int mode, double ta, double tb, double ca, double cb,
                      double shift, int maskpow, double tmask, void* col_base = nullptr, const double* tlist = nullptr,
-                     int count = 1) {
+                     int count = 1, const double* ca_vec = nullptr, const double* shift_vec = nullptr) {
   int ncol = h->nc, nrow = h->nr, roll = 0;
   double dcol, drow;
   const aw_config& c = h->cfg;
@@ -514,23 +572,31 @@ static int build_tab(aw_state_s* h, int slot, int fn, int mode, double ta, doubl
   } else {
     dcol = drow = fn == 0 ? c.dX : c.dP;
   }
-  void* col = col_base ? col_base : tab_col(h, slot);
+  long long istride = (long long)TAB_NSLOT * (h->nc + h->nr);
+  void* col = col_base ? col_base : at_inst(tab_col(h, slot), istride, h->esz, h->v0);
   void* row = (char*)col + (size_t)h->nc * h->esz;
   int f32 = tab_fmt(h);
   long long tstride = (long long)h->nc + h->nr;
+  const double* prm = h->np ? (const double*)h->params.p + (size_t)h->v0 * h->np : nullptr;
+  int np = h->np;
+  if (ca_vec) ca_vec += h->v0;
+  if (shift_vec) shift_vec += h->v0;
   void* args[] = {&col, &row, &f32, &fn, &mode, &ncol, &dcol, &roll, &nrow, &drow,
-                  &ta, &tb, &ca, &cb, &shift, &maskpow, &tmask, &tlist, &tstride};
+                  &ta, &tb, &ca, &cb, &shift, &maskpow, &tmask, &tlist, &tstride,
+                  &prm, &np, &ca_vec, &shift_vec, &istride};
   const int n = ncol + nrow;
-  return hjit(h, h->k_tab, dim3((n + 31) / 32, count), dim3(32), args);
+  return hjit(h, h->k_tab, dim3((n + 31) / 32, count, col_base ? 1 : h->vc), dim3(32), args);
 }
 
 static int build_mask2d(aw_state_s* h, int which, double t) {
   DevBuf& m = which == 0 ? h->maskx : h->maskp;
-  void* out = m.p;
+  void* out = at_inst(m.p, gsz(h), h->f32 ? 4 : 8, h->v0);
   int f32 = tab_fmt(h), nr = h->nr, nc = h->nc;
   double a = h->cfg.dXX, b = h->cfg.dXX_prime, c = h->cfg.dPP, d = h->cfg.dPP_prime;
-  void* args[] = {&out, &f32, &which, &t, &nr, &nc, &a, &b, &c, &d};
-  return hjit(h, h->k_mask2d, dim3((nc + 127) / 128, nr), dim3(128), args);
+  const double* prm = h->np ? (const double*)h->params.p + (size_t)h->v0 * h->np : nullptr;
+  int np = h->np;
+  void* args[] = {&out, &f32, &which, &t, &nr, &nc, &a, &b, &c, &d, &prm, &np};
+  return hjit(h, h->k_mask2d, dim3((nc + 127) / 128, nr, h->vc), dim3(128), args);
 }
 
 // sum over a buffer (mode as aw_k_partial); result in out[0..1]
@@ -550,7 +616,6 @@ static int dsum(aw_state_s* h, const void* p, long long n, int mode, long long s
   return AW_OK;
 }
 
-static double* dscal(aw_state_s* h, int k) { return (double*)h->scal.p + k; }
 
 // ============================================================================ creation
 // error message setter for the other translation units of the library (C++ linkage, not exported API)
@@ -561,6 +626,68 @@ extern "C" const char* aw_last_error(void) { return g_err.c_str(); }
 extern "C" int64_t aw_launch_count(void) { return g_launches.load(); }
 
 static std::string cstr(const char* s, const char* dflt) { return s ? std::string(s) : std::string(dflt); }
+
+// Bloch minima of instance i: min over (V(x) + V(x')) = min V(x) + min V(x') since rounding is
+// monotone (the reference's V_min / K_min, wigner_bloch_cuda_1d.py:55-92)
+static int bloch_minima(aw_state_s* h, int i) {
+  const aw_config* cfg = &h->cfg;
+  const int nmax = std::max(h->nr, h->nc);
+  TRY(dalloc(h->stage, (size_t)4 * nmax * 8));
+  double* d = (double*)h->stage.p;
+  const double* prm = h->np ? (const double*)h->params.p + (size_t)i * h->np : nullptr;
+  auto eval = [&](int fn, int n, double dx, double* out) -> int {
+    void* o = out;
+    double tt = cfg->t_initial;
+    int np = h->np;
+    long long ostride = 0;
+    void* args[] = {&o, &fn, &n, &dx, &tt, &prm, &np, &ostride};
+    return hjit(h, h->k_values, dim3((n + 255) / 256), dim3(256), args);
+  };
+  if (h->kind == AW_WIGNER_BLOCH) {
+    TRY(eval(0, h->nc, cfg->dXX, d));
+    TRY(eval(0, h->nr, cfg->dXX_prime, d + nmax));
+    TRY(eval(1, h->nc, cfg->dPP, d + 2 * nmax));
+    TRY(eval(1, h->nr, cfg->dPP_prime, d + 3 * nmax));
+  } else {
+    TRY(eval(0, h->nc, cfg->dX, d));
+    TRY(eval(0, h->nr, cfg->dX, d + nmax));
+    TRY(eval(1, h->nc, cfg->dP, d + 2 * nmax));
+    TRY(eval(1, h->nr, cfg->dP, d + 3 * nmax));
+  }
+  std::vector<double> hv(4 * (size_t)nmax);
+  CK(cudaMemcpyAsync(hv.data(), d, hv.size() * 8, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  double v1 = INFINITY, v2 = INFINITY, k1 = INFINITY, k2 = INFINITY;
+  bool knan = false;
+  for (int j = 0; j < h->nc; ++j) v1 = std::min(v1, hv[j]);
+  for (int r = 0; r < h->nr; ++r) v2 = std::min(v2, hv[nmax + r]);
+  for (int j = 0; j < h->nc; ++j) { k1 = std::min(k1, hv[2 * nmax + j]); knan |= !std::isfinite(hv[2 * nmax + j]); }
+  for (int r = 0; r < h->nr; ++r) { k2 = std::min(k2, hv[3 * nmax + r]); knan |= !std::isfinite(hv[3 * nmax + r]); }
+  double km = k1 + k2;
+  if (h->kind == AW_RHO_BLOCH) km = knan ? NAN : 0.0;  // fill_K multiplies a zeroed array (rho_bloch_cuda_1d.py:370)
+  h->vmin_i[i] = define_round(v1 + v2);
+  h->kmin_i[i] = define_round(km);
+  h->minima_ok[i] = 1;
+  return AW_OK;
+}
+
+// Bloch coefficients of the view's instances for steps of dbeta[k] (k = 0 .. vc-1)
+static int upload_bloch(aw_state_s* h, const double* dbeta) {
+  std::vector<double> v(4 * (size_t)h->ni);
+  CK(cudaMemcpyAsync(v.data(), h->bvec.p, v.size() * 8, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (int k = 0; k < h->vc; ++k) {
+    const int i = h->v0 + k;
+    if (!h->minima_ok[i]) TRY(bloch_minima(h, i));
+    v[i] = -0.25 * dbeta[k];
+    v[h->ni + i] = 0.5 * h->vmin_i[i];
+    v[2 * h->ni + i] = -0.5 * dbeta[k];
+    v[3 * h->ni + i] = 0.5 * h->kmin_i[i];
+  }
+  CK(cudaMemcpyAsync(h->bvec.p, v.data(), v.size() * 8, cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return AW_OK;
+}
 
 static int create_impl(const aw_config* cfg, aw_state_s* h) {
   h->cfg = *cfg;
@@ -610,6 +737,36 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   if (h->nc < 32 || h->nc > maxn || (!h->kn.sw && (h->nr < 32 || h->nr > maxn)) || (h->wn && h->wn > 8192))
     return fail(AW_E_ARG, "grid sides must be powers of two in [32, %d] (Wigner grid up to 8192)", maxn);
 
+  // batch
+  h->ni = std::max(1, (int)cfg->n_inst);
+  h->np = std::max(0, (int)cfg->n_params);
+  h->v0 = 0;
+  h->vc = h->ni;
+  for (int k = 0; k < h->np; ++k) {
+    const char* nm = cfg->param_names ? cfg->param_names[k] : nullptr;
+    if (!nm || !*nm) return fail(AW_E_ARG, "parameter %d has no name", k);
+    static const char* reserved[] = {"X", "P", "XX", "XX_prime", "PP", "PP_prime", "X_prime", "P_prime", "t", "i",
+                                     "j", "dX", "dP", "M_PI"};
+    for (const char* r : reserved)
+      if (!strcmp(nm, r)) return fail(AW_E_ARG, "parameter name %s is taken by the kernels", nm);
+    for (const char* c = nm; *c; ++c)
+      if (!(isalnum((unsigned char)*c) || *c == '_') || (c == nm && isdigit((unsigned char)*c)))
+        return fail(AW_E_ARG, "parameter name %s is not an identifier", nm);
+    h->pnames.push_back(nm);
+  }
+  h->init_expr = cstr(cfg->init_expr, "");
+  if (h->ni > 1) {
+    if (h->kn.sw) return fail(AW_E_ARG, "batches exist for the Wigner-Moyal, Wigner-Bloch, von Neumann and rho-Bloch propagators");
+    if (cfg->v_time_dependent || cfg->k_time_dependent || cfg->absx_mode == 2 || cfg->absp_mode == 2)
+      return fail(AW_E_ARG, "a batch needs V, K and absorbing boundaries that do not depend on t");
+    if (h->kn.vn && cfg->ehrenfest)
+      return fail(AW_E_ARG, "von Neumann batches record trace and purity only (no per-step Ehrenfest observables)");
+  }
+  h->active.assign(h->ni, 1);
+  h->vmin_i.assign(h->ni, 0.0);
+  h->kmin_i.assign(h->ni, 0.0);
+  h->minima_ok.assign(h->ni, 0);
+
   CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
   if (h->kn.rotated) {
     CK(cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking));
@@ -620,9 +777,11 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   }
 
   // user module
-  std::string src = awjit::module_source(h->kn, h->consts, h->V, h->K, h->absx, h->absp, h->obs_x, h->obs_p);
+  std::string src = awjit::module_source(h->kn, h->consts, h->V, h->K, h->absx, h->absp, h->obs_x, h->obs_p,
+                                         h->pnames, h->init_expr);
   TRY(jit_compile(src, &h->lib));
   TRY(jit_kernel(h->lib, "aw_tab", &h->k_tab));
+  if (!h->init_expr.empty()) TRY(jit_kernel(h->lib, "aw_binit", &h->k_binit));
   TRY(jit_kernel(h->lib, "aw_values", &h->k_values));
   TRY(jit_kernel(h->lib, "aw_finalize", &h->k_final));
   if (h->kn.rotated) {
@@ -631,19 +790,27 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   }
 
   // buffers
+  const size_t ni = h->ni;
   const size_t grid = (size_t)(h->kn.sw ? h->sw_rows : h->nr) * h->nc;
   const size_t wgrid = h->kn.rotated ? grid : (size_t)h->wn * h->wn;
-  TRY(dalloc(h->rho, grid * h->esz));
-  TRY(dalloc(h->W, wgrid * h->esz));
-  TRY(dalloc(h->tmp, std::max(grid, wgrid) * 16));
-  CK(cudaMemset(h->rho.p, 0, grid * h->esz));
-  CK(cudaMemset(h->W.p, 0, wgrid * h->esz));
-  TRY(dalloc(h->tabs, (size_t)TAB_NSLOT * (h->nc + h->nr) * h->esz));
-  TRY(dalloc(h->scal, 2048 * sizeof(double)));
-  TRY(dalloc(h->stop, 16 * sizeof(int)));
+  TRY(dalloc(h->rho, ni * grid * h->esz));
+  TRY(dalloc(h->W, ni * wgrid * h->esz));
+  TRY(dalloc(h->tmp, std::max(ni * grid, wgrid) * 16));
+  CK(cudaMemset(h->rho.p, 0, ni * grid * h->esz));
+  CK(cudaMemset(h->W.p, 0, ni * wgrid * h->esz));
+  TRY(dalloc(h->tabs, ni * TAB_NSLOT * (h->nc + h->nr) * h->esz));
+  const size_t nscal = 2 * ni + 16 + ni * FIN_TV;
+  TRY(dalloc(h->scal, nscal * sizeof(double)));
+  TRY(dalloc(h->stop, 2 * ni * sizeof(int)));
   TRY(dalloc(h->part, 1024 * sizeof(double2)));
-  CK(cudaMemset(h->scal.p, 0, 2048 * sizeof(double)));
-  CK(cudaMemset(h->stop.p, 0, 16 * sizeof(int)));
+  CK(cudaMemset(h->scal.p, 0, nscal * sizeof(double)));
+  CK(cudaMemset(h->stop.p, 0, 2 * ni * sizeof(int)));
+  TRY(dalloc(h->bvec, 4 * ni * sizeof(double)));
+  CK(cudaMemset(h->bvec.p, 0, 4 * ni * sizeof(double)));
+  if (h->np) {
+    TRY(dalloc(h->params, ni * h->np * sizeof(double)));
+    CK(cudaMemset(h->params.p, 0, ni * h->np * sizeof(double)));
+  }
   {
     // term tables: int slot[64], kind[64], idx[64], double coef[64]
     TRY(dalloc(h->terms, 64 * 3 * sizeof(int) + 64 * sizeof(double)));
@@ -698,13 +865,20 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   // reduction scratch of the Wigner column pass
   const int wr = h->kn.rotated ? h->nr : h->wn, wc = h->kn.rotated ? h->nc : h->wn;
   h->red_blocks = aw_col_pass_blocks(wr, wc, h->f32);
+  if (h->ni > 1) {
+    // a batch splits its columns the same way in every launch, chosen for the full batch
+    h->col_lines = aw_col_pass_lines(h->nr, h->nc, h->ni, h->f32);
+    if (h->col_lines <= 0) return fail(AW_E_ARG, "unsupported batch grid %d x %d", h->nr, h->nc);
+    if (h->kn.rotated) h->red_blocks = h->nc / h->col_lines;
+  }
   if (h->red_blocks <= 0) return fail(AW_E_ARG, "unsupported Wigner grid %d x %d", wr, wc);
-  TRY(dalloc(h->red_line, (size_t)wc * 8));
-  TRY(dalloc(h->red_cross, (size_t)h->red_blocks * wr * 8));
-  TRY(dalloc(h->red_sq, (size_t)h->red_blocks * 8));
+  // per-instance reduction scratch (the pass kernels index it by instance)
+  TRY(dalloc(h->red_line, ni * (size_t)wc * 8));
+  TRY(dalloc(h->red_cross, ni * (size_t)h->red_blocks * wr * 8));
+  TRY(dalloc(h->red_sq, ni * (size_t)h->red_blocks * 8));
   TRY(dalloc(h->rowsum, (size_t)std::max(wr, wc) * 8));
-  TRY(dalloc(h->diag, (size_t)std::max(h->nr, h->nc) * 16));
-  TRY(dalloc(h->abs2, 2 * (size_t)std::max(h->nr, 1) * 8));  // two parities, see rot_run
+  TRY(dalloc(h->diag, ni * (size_t)std::max(h->nr, h->nc) * 16));
+  TRY(dalloc(h->abs2, 2 * ni * (size_t)std::max(h->nr, 1) * 8));  // two parities, see rot_run
   if (h->kn.rotated) {
     // the marginal column pass: narrow slabs spread over every SM, row partials summed across
     // clusters of 8 blocks in distributed shared memory, so that z_blocks stays small
@@ -713,54 +887,21 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
     h->z_cluster = (h->nc / h->z_lines) % 8 == 0 && h->nr % 8 == 0 && z_smem <= 160 * 1024 ? 8 : 1;
     h->z_blocks = h->nc / h->z_lines / h->z_cluster;
     // two parities, so that step n's reduction can run while step n + 1 writes the other
-    TRY(dalloc(h->zbuf, 2 * (size_t)(h->nc + h->nr) * 16));
-    TRY(dalloc(h->altbuf, 2 * (size_t)h->z_blocks * h->nr * 16));
+    TRY(dalloc(h->zbuf, 2 * ni * (size_t)(h->nc + h->nr) * 16));
+    TRY(dalloc(h->altbuf, 2 * ni * (size_t)h->z_blocks * h->nr * 16));
   }
 
-  // 2-D absorbing masks of the rotated frame
+  // 2-D absorbing masks of the rotated frame (one per instance)
   if (h->kn.rotated) {
-    if (cfg->absx_mode) TRY(dalloc(h->maskx, grid * (h->f32 ? 4 : 8)));
-    if (cfg->absp_mode) TRY(dalloc(h->maskp, grid * (h->f32 ? 4 : 8)));
+    if (cfg->absx_mode) TRY(dalloc(h->maskx, ni * grid * (h->f32 ? 4 : 8)));
+    if (cfg->absp_mode) TRY(dalloc(h->maskp, ni * grid * (h->f32 ? 4 : 8)));
   }
 
-  // Bloch minima: min over (V(x) + V(x')) = min V(x) + min V(x') since rounding is monotone
   if (h->kind == AW_WIGNER_BLOCH || h->kind == AW_RHO_BLOCH) {
-    double vm = 0.0, km = 0.0;
-    const int nmax = std::max(h->nr, h->nc);
-    TRY(dalloc(h->stage, (size_t)4 * nmax * 8));
-    double* d = (double*)h->stage.p;
-    auto eval = [&](int fn, int n, double dx, double* out) -> int {
-      void* o = out;
-      double tt = cfg->t_initial;
-      void* args[] = {&o, &fn, &n, &dx, &tt};
-      return hjit(h, h->k_values, dim3((n + 255) / 256), dim3(256), args);
-    };
-    std::vector<double> a(nmax), b(nmax);
-    if (h->kind == AW_WIGNER_BLOCH) {
-      TRY(eval(0, h->nc, cfg->dXX, d));
-      TRY(eval(0, h->nr, cfg->dXX_prime, d + nmax));
-      TRY(eval(1, h->nc, cfg->dPP, d + 2 * nmax));
-      TRY(eval(1, h->nr, cfg->dPP_prime, d + 3 * nmax));
-    } else {
-      TRY(eval(0, h->nc, cfg->dX, d));
-      TRY(eval(0, h->nr, cfg->dX, d + nmax));
-      TRY(eval(1, h->nc, cfg->dP, d + 2 * nmax));
-      TRY(eval(1, h->nr, cfg->dP, d + 3 * nmax));
-    }
-    std::vector<double> hv(4 * (size_t)nmax);
-    CK(cudaMemcpyAsync(hv.data(), d, hv.size() * 8, cudaMemcpyDeviceToHost, h->st));
-    CK(cudaStreamSynchronize(h->st));
-    double v1 = INFINITY, v2 = INFINITY, k1 = INFINITY, k2 = INFINITY;
-    bool knan = false;
-    for (int j = 0; j < h->nc; ++j) v1 = std::min(v1, hv[j]);
-    for (int i = 0; i < h->nr; ++i) v2 = std::min(v2, hv[nmax + i]);
-    for (int j = 0; j < h->nc; ++j) { k1 = std::min(k1, hv[2 * nmax + j]); knan |= !std::isfinite(hv[2 * nmax + j]); }
-    for (int i = 0; i < h->nr; ++i) { k2 = std::min(k2, hv[3 * nmax + i]); knan |= !std::isfinite(hv[3 * nmax + i]); }
-    vm = v1 + v2;
-    km = k1 + k2;
-    if (h->kind == AW_RHO_BLOCH) km = knan ? NAN : 0.0;  // fill_K multiplies a zeroed array (rho_bloch_cuda_1d.py:370)
-    h->V_min = define_round(vm);
-    h->K_min = define_round(km);
+    // minima of every instance (a batch recomputes an instance's after aw_set_params)
+    for (int i = 0; i < h->ni; ++i) TRY(bloch_minima(h, i));
+    h->V_min = h->vmin_i[0];
+    h->K_min = h->kmin_i[0];
   }
   CK(cudaStreamSynchronize(h->st));
   return AW_OK;
@@ -823,33 +964,56 @@ extern "C" int aw_bloch_min(aw_handle h, double* v_min, double* k_min) {
 }
 
 // ============================================================================ buffers
-static DevBuf* buf_of(aw_state_s* h, int which, long long* rows, long long* cols) {
+// A state buffer of the view: pointer to its first instance's data, rows = view instances x rows
+// of one instance.  *base (optional) receives the whole buffer.
+static void* buf_of(aw_state_s* h, int which, long long* rows, long long* cols, DevBuf** base = nullptr) {
+  DevBuf* b = nullptr;
+  long long r = 0, c = 0;
   switch (which) {
     case AW_BUF_RHO:
     case AW_BUF_PSI:
       if ((which == AW_BUF_PSI) != h->kn.sw) return nullptr;
-      *rows = h->nr;
-      *cols = h->nc;
-      return &h->rho;
+      r = h->nr;
+      c = h->nc;
+      b = &h->rho;
+      break;
     case AW_BUF_WIGNER:
-      *rows = h->kn.rotated ? h->nr : h->wn;
-      *cols = h->kn.rotated ? h->nc : h->wn;
-      return &h->W;
+      r = h->kn.rotated ? h->nr : h->wn;
+      c = h->kn.rotated ? h->nc : h->wn;
+      b = &h->W;
+      break;
     case AW_BUF_SNAPSHOT:
-      *rows = h->nr;
-      *cols = h->nc;
-      return &h->snap;
+      r = h->nr;
+      c = h->nc;
+      b = &h->snap;
+      break;
     default:
       return nullptr;
   }
+  if (base) *base = b;
+  *rows = r * h->vc;
+  *cols = c;
+  if (!b->p) return nullptr;  // the snapshot before its first write
+  return at_inst(b->p, r * c, h->esz, h->v0);
+}
+
+static int clear_stops(aw_state_s* h);
+
+// snapshot storage for every instance, allocated on first use
+static int ensure_snap(aw_state_s* h) {
+  if (h->snap.p) return AW_OK;
+  TRY(dalloc(h->snap, (size_t)h->ni * gsz(h) * h->esz));
+  CK(cudaMemset(h->snap.p, 0, (size_t)h->ni * gsz(h) * h->esz));
+  return AW_OK;
 }
 
 extern "C" int aw_buffer(aw_handle h, int32_t which, void** dptr, int64_t* rows, int64_t* cols, int32_t* elem_bytes) {
   if (!h) return fail(AW_E_ARG, "null handle");
   long long r, c;
-  DevBuf* b = buf_of(h, which, &r, &c);
-  if (!b) return fail(AW_E_ARG, "no buffer %d for this propagator", which);
-  if (dptr) *dptr = b->p;
+  if (which == AW_BUF_SNAPSHOT) TRY(ensure_snap(h));
+  void* p = buf_of(h, which, &r, &c);
+  if (!p) return fail(AW_E_ARG, "no buffer %d for this propagator", which);
+  if (dptr) *dptr = p;
   if (rows) *rows = r;
   if (cols) *cols = c;
   if (elem_bytes) *elem_bytes = h->esz;
@@ -859,15 +1023,21 @@ extern "C" int aw_buffer(aw_handle h, int32_t which, void** dptr, int64_t* rows,
 extern "C" int aw_set_buffer(aw_handle h, int32_t which, const void* src, int32_t src_on_device) {
   if (!h || !src) return fail(AW_E_ARG, "null argument");
   long long r, c;
-  DevBuf* b = buf_of(h, which, &r, &c);
+  if (which == AW_BUF_SNAPSHOT) TRY(ensure_snap(h));
+  void* b = buf_of(h, which, &r, &c);
   if (!b) return fail(AW_E_ARG, "no buffer %d for this propagator", which);
-  if (which == AW_BUF_SNAPSHOT) TRY(dalloc(h->snap, (size_t)r * c * h->esz));
   const size_t n = (size_t)r * c;
   if (!h->f32) {
-    CK(cudaMemcpyAsync(b->p, src, n * 16, src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(b, src, n * 16, src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->st));
   } else {
-    CK(cudaMemcpyAsync(h->tmp.p, src, n * 16, src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->st));
-    KL(aw_k_convert(h->tmp.p, 0, b->p, 1, (long long)n, h->st));
+    for (size_t off = 0; off < n;) {
+      // through the complex128 scratch, at most its size at a time
+      const size_t m = std::min(n - off, h->tmp.bytes / 16);
+      CK(cudaMemcpyAsync(h->tmp.p, (const char*)src + off * 16, m * 16,
+                         src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->st));
+      KL(aw_k_convert(h->tmp.p, 0, (char*)b + off * 8, 1, (long long)m, h->st));
+      off += m;
+    }
   }
   CK(cudaStreamSynchronize(h->st));
   return AW_OK;
@@ -876,15 +1046,20 @@ extern "C" int aw_set_buffer(aw_handle h, int32_t which, const void* src, int32_
 extern "C" int aw_get_buffer(aw_handle h, int32_t which, void* dst, int32_t dst_on_device) {
   if (!h || !dst) return fail(AW_E_ARG, "null argument");
   long long r, c;
-  DevBuf* b = buf_of(h, which, &r, &c);
-  if (!b || !b->p) return fail(AW_E_ARG, "no buffer %d for this propagator", which);
+  void* b = buf_of(h, which, &r, &c);
+  if (!b) return fail(AW_E_ARG, "no buffer %d for this propagator", which);
   const size_t n = (size_t)r * c;
-  const void* from = b->p;
-  if (h->f32) {
-    KL(aw_k_convert(b->p, 1, h->tmp.p, 0, (long long)n, h->st));
-    from = h->tmp.p;
+  if (!h->f32) {
+    CK(cudaMemcpyAsync(dst, b, n * 16, dst_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->st));
+  } else {
+    for (size_t off = 0; off < n;) {
+      const size_t m = std::min(n - off, h->tmp.bytes / 16);
+      KL(aw_k_convert((char*)b + off * 8, 1, h->tmp.p, 0, (long long)m, h->st));
+      CK(cudaMemcpyAsync((char*)dst + off * 16, h->tmp.p, m * 16,
+                         dst_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->st));
+      off += m;
+    }
   }
-  CK(cudaMemcpyAsync(dst, from, n * 16, dst_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   return AW_OK;
 }
@@ -892,48 +1067,51 @@ extern "C" int aw_get_buffer(aw_handle h, int32_t which, void* dst, int32_t dst_
 extern "C" int aw_copy_buffer(aw_handle h, int32_t from, int32_t to) {
   if (!h) return fail(AW_E_ARG, "null handle");
   long long r1, c1, r2, c2;
-  DevBuf* a = buf_of(h, from, &r1, &c1);
-  DevBuf* b = buf_of(h, to, &r2, &c2);
-  if (!a || !b || r1 * c1 != r2 * c2) return fail(AW_E_ARG, "incompatible buffers %d -> %d", from, to);
-  if (to == AW_BUF_SNAPSHOT) TRY(dalloc(h->snap, (size_t)r2 * c2 * h->esz));
-  if (!a->p) return fail(AW_E_STATE, "buffer %d is empty", from);
-  CK(cudaMemcpyAsync(b->p, a->p, (size_t)r1 * c1 * h->esz, cudaMemcpyDeviceToDevice, h->st));
+  if (to == AW_BUF_SNAPSHOT) TRY(ensure_snap(h));
+  void* a = buf_of(h, from, &r1, &c1);
+  void* b = buf_of(h, to, &r2, &c2);
+  if (!a || !b || r1 * c1 != r2 * c2) return fail(AW_E_ARG, "incompatible or empty buffers %d -> %d", from, to);
+  CK(cudaMemcpyAsync(b, a, (size_t)r1 * c1 * h->esz, cudaMemcpyDeviceToDevice, h->st));
   return AW_OK;
 }
 
 extern "C" int aw_fill_const(aw_handle h, int32_t which, double re, double im) {
   if (!h) return fail(AW_E_ARG, "null handle");
   long long r, c;
-  DevBuf* b = buf_of(h, which, &r, &c);
+  if (which == AW_BUF_SNAPSHOT) TRY(ensure_snap(h));
+  void* b = buf_of(h, which, &r, &c);
   if (!b) return fail(AW_E_ARG, "no buffer %d", which);
-  KL(aw_k_fill(b->p, h->f32, r * c, re, im, h->st));
+  KL(aw_k_fill(b, h->f32, r * c, re, im, h->st));
   return AW_OK;
 }
 
 extern "C" int aw_fill_expr(aw_handle h, int32_t which, const char* expr) {
   if (!h || !expr) return fail(AW_E_ARG, "null argument");
   long long r, c;
-  DevBuf* b = buf_of(h, which, &r, &c);
+  if (which == AW_BUF_SNAPSHOT) TRY(ensure_snap(h));
+  void* b = buf_of(h, which, &r, &c);
   if (!b) return fail(AW_E_ARG, "no buffer %d", which);
   cudaLibrary_t lib;
   TRY(jit_compile(awjit::init_source(h->kn, h->consts, expr), &lib));
   cudaKernel_t k;
   TRY(jit_kernel(lib, "aw_init", &k));
-  void* out = b->p;
-  int f32 = h->f32, nr = (int)r, nc = (int)c;
+  int f32 = h->f32, nr = (int)(r / h->vc), nc = (int)c;
   double dX = h->cfg.dX, dP = h->cfg.dP;
-  void* args[] = {&out, &f32, &nr, &nc, &dX, &dP};
-  TRY(hjit(h, k, dim3((nc + 127) / 128, h->kn.sw ? 1 : nr), dim3(128), args));
+  for (int q = 0; q < h->vc; ++q) {
+    void* out = (char*)b + (size_t)q * nr * nc * h->esz;
+    void* args[] = {&out, &f32, &nr, &nc, &dX, &dP};
+    TRY(hjit(h, k, dim3((nc + 127) / 128, h->kn.sw ? 1 : nr), dim3(128), args));
+  }
   return AW_OK;
 }
 
 extern "C" int aw_sum(aw_handle h, int32_t which, double* re, double* im) {
   if (!h) return fail(AW_E_ARG, "null handle");
   long long r, c;
-  DevBuf* b = buf_of(h, which, &r, &c);
+  void* b = buf_of(h, which, &r, &c);
   if (!b) return fail(AW_E_ARG, "no buffer %d", which);
   double s[2];
-  TRY(dsum(h, b->p, r * c, 0, 0, s));
+  TRY(dsum(h, b, r * c, 0, 0, s));
   if (re) *re = s[0];
   if (im) *im = s[1];
   return AW_OK;
@@ -943,7 +1121,7 @@ extern "C" int aw_trace(aw_handle h, double* re, double* im) {
   if (!h) return fail(AW_E_ARG, "null handle");
   if (h->nr != h->nc) return fail(AW_E_STATE, "trace of a non-square grid");
   double s[2];
-  TRY(dsum(h, h->rho.p, h->nr, 3, h->nc + 1, s));
+  TRY(dsum(h, at_inst(h->rho.p, gsz(h), h->esz, h->v0), h->nr, 3, h->nc + 1, s));
   if (re) *re = s[0];
   if (im) *im = s[1];
   return AW_OK;
@@ -952,9 +1130,9 @@ extern "C" int aw_trace(aw_handle h, double* re, double* im) {
 extern "C" int aw_scale(aw_handle h, int32_t which, double re, double im) {
   if (!h) return fail(AW_E_ARG, "null handle");
   long long r, c;
-  DevBuf* b = buf_of(h, which, &r, &c);
+  void* b = buf_of(h, which, &r, &c);
   if (!b) return fail(AW_E_ARG, "no buffer %d", which);
-  KL(aw_k_scale(b->p, h->f32, r * c, re, im, nullptr, h->st));
+  KL(aw_k_scale(b, h->f32, r * c, re, im, nullptr, h->st));
   return AW_OK;
 }
 
@@ -1039,6 +1217,8 @@ static int wigner_passes(aw_state_s* h, const WignerGrid& g, const void* first_i
   AwPassArgs a = pnone(h);
   a.nrows = g.nr;
   a.ncols = g.nc;
+  a.batch_elems = (long long)g.nr * g.nc;
+  a.batch_tab = 0;  // the Blackman tables are shared by all instances
   void* bcol = blackman ? h->blk_tabs.p : nullptr;
   void* brow = blackman ? (char*)h->blk_tabs.p + (size_t)g.nc * h->esz : nullptr;
   if (!row_first_done) {
@@ -1057,6 +1237,8 @@ static int wigner_passes(aw_state_s* h, const WignerGrid& g, const void* first_i
   a = pnone(h);
   a.nrows = g.nr;
   a.ncols = g.nc;
+  a.batch_elems = (long long)g.nr * g.nc;
+  a.batch_tab = 0;  // the Blackman tables are shared by all instances
   a.in = a.out = g.buf;
   if (blackman) {
     a.f0.row_tab = brow;
@@ -1069,6 +1251,8 @@ static int wigner_passes(aw_state_s* h, const WignerGrid& g, const void* first_i
   a = pnone(h);
   a.nrows = g.nr;
   a.ncols = g.nc;
+  a.batch_elems = (long long)g.nr * g.nc;
+  a.batch_tab = 0;  // the Blackman tables are shared by all instances
   a.in = a.out = g.buf;
   if (blackman) {
     a.f0.col_tab = bcol;
@@ -1081,6 +1265,8 @@ static int wigner_passes(aw_state_s* h, const WignerGrid& g, const void* first_i
   a = pnone(h);
   a.nrows = g.nr;
   a.ncols = g.nc;
+  a.batch_elems = (long long)g.nr * g.nc;
+  a.batch_tab = 0;  // the Blackman tables are shared by all instances
   a.in = g.buf;
   a.out = store_last ? g.buf : nullptr;
   if (blackman) {
@@ -1113,6 +1299,7 @@ struct FinalArgs {
   int sqrt_norm;
 };
 
+// one instance (the first of the view): the argument pointers already point at its data
 static int launch_finalize_args(aw_state_s* h, const FinalArgs& f, double t, double* hist_row, int stop_on_purity) {
   const double* colsum = f.colsum;
   const double* rowpart = f.rowpart;
@@ -1120,7 +1307,8 @@ static int launch_finalize_args(aw_state_s* h, const FinalArgs& f, double t, dou
   const double* sqpart = f.sqpart;
   double* rowsum = (double*)h->rowsum.p;
   double* inv = f.inv;
-  int* stop = (int*)h->stop.p;
+  int* stop = dstop(h, h->v0);
+  const double* prm = h->np ? (const double*)h->params.p + (size_t)h->v0 * h->np : nullptr;
   int ncol = f.ncol, nrow = f.nrow;
   double dX = h->cfg.dX, dP = h->cfg.dP, dXdP = f.dXdP;
   const int* ts = (const int*)h->terms.p;
@@ -1130,33 +1318,45 @@ static int launch_finalize_args(aw_state_s* h, const FinalArgs& f, double t, dou
   int nterms = (int)h->tslot.size(), nslots = h->cfg.n_slots;
   int cstride = f.cstride, proll = f.proll, pown = f.pnorm_own, sq = f.sqrt_norm;
   void* args[] = {&colsum, &rowpart, &nparts, &sqpart, &rowsum, &hist_row, &inv, &stop, &stop_on_purity, &t,
-                  &ncol, &nrow, &dX, &dP, &dXdP, &ts, &tk, &ti, &tc, &nterms, &nslots, &cstride, &proll, &pown, &sq};
+                  &ncol, &nrow, &dX, &dP, &dXdP, &ts, &tk, &ti, &tc, &nterms, &nslots, &cstride, &proll, &pown, &sq,
+                  &prm};
   return hjit(h, h->k_final, dim3(1), dim3(256), args);
 }
 
 // rotated frame: marginals of W from the reducing column pass
 static int launch_finalize(aw_state_s* h, double t, double* hist_row, int stop_on_purity) {
-  FinalArgs f{(const double*)h->red_line.p, 1, h->nc, (const double*)h->red_cross.p, h->red_blocks, h->nr, 0,
-              (const double*)h->red_sq.p, h->cfg.dXdP, dscal(h, 0), 0, 0};
+  const int i = h->v0;
+  FinalArgs f{(const double*)h->red_line.p + (size_t)i * h->nc, 1, h->nc,
+              (const double*)h->red_cross.p + (size_t)i * h->red_blocks * h->nr, h->red_blocks, h->nr, 0,
+              (const double*)h->red_sq.p + (size_t)i * h->red_blocks, h->cfg.dXdP, dinv(h, i), 0, 0};
   return launch_finalize_args(h, f, t, hist_row, stop_on_purity);
 }
 
-// marginal buffers of parity par (zbuf, altbuf, abs2 hold two sets)
-static double2* zbuf_of(aw_state_s* h, int par) { return (double2*)h->zbuf.p + (size_t)par * (h->nc + h->nr); }
-static double2* altbuf_of(aw_state_s* h, int par) { return (double2*)h->altbuf.p + (size_t)par * h->z_blocks * h->nr; }
-static double* abs2_of(aw_state_s* h, int par) { return (double*)h->abs2.p + (size_t)par * std::max(h->nr, 1); }
+// marginal buffers of parity par (zbuf, altbuf, abs2 hold two sets, each for every instance)
+static double2* zbuf_of(aw_state_s* h, int par) { return (double2*)h->zbuf.p + (size_t)par * h->ni * (h->nc + h->nr); }
+static double2* altbuf_of(aw_state_s* h, int par) {
+  return (double2*)h->altbuf.p + (size_t)par * h->ni * h->z_blocks * h->nr;
+}
+static double* abs2_of(aw_state_s* h, int par) { return (double*)h->abs2.p + (size_t)par * h->ni * std::max(h->nr, 1); }
+// observable rows of instance i
+static double* hist_of(aw_state_s* h, int i) { return (double*)h->hist.p + (size_t)i * h->hist_cap * h->hist_cols; }
 
 static int launch_finalize_rot(aw_state_s* h, double t, double* hist_row, int stop_on_purity, int par = 0,
                                cudaStream_t st = nullptr) {
-  const double2* z = zbuf_of(h, par);
-  const double2* wpart = altbuf_of(h, par);
+  // every instance of the view: blockIdx.y = instance - v0
+  const int i0 = h->v0;
   int nparts = h->z_blocks;
-  const double* abs2 = abs2_of(h, par);
   int nb2 = aw_row_pass_blocks(h->nr, h->nc, h->f32);
-  double* tv = dscal(h, 16);
-  unsigned int* counter = (unsigned int*)h->stop.p + 1;
-  double* inv = dscal(h, 0);
-  int* stop = (int*)h->stop.p;
+  const double2* z = zbuf_of(h, par) + (size_t)i0 * h->nc;
+  const double2* wpart = altbuf_of(h, par) + (size_t)i0 * nparts * h->nr;
+  const double* abs2 = abs2_of(h, par) + (size_t)i0 * nb2;
+  double* tv = dtv(h, i0);
+  unsigned int* counter = dcounter(h, i0);
+  double* inv = dinv(h, i0);
+  int* stop = dstop(h, i0);
+  const double* prm = h->np ? (const double*)h->params.p + (size_t)i0 * h->np : nullptr;
+  int np = h->np;
+  long long hstride = h->hist_cap * h->hist_cols;
   int ncol = h->nc, nrow = h->nr;
   double dX = h->cfg.dX, dP = h->cfg.dP, dXdP = h->cfg.dXdP;
   const int* ts = (const int*)h->terms.p;
@@ -1168,33 +1368,52 @@ static int launch_finalize_rot(aw_state_s* h, double t, double* hist_row, int st
   int nchunk = 16;
   while (nchunk > 1 && ((std::min(ncol, nrow) % nchunk) || (nterms + 2) * nchunk > 1024)) nchunk >>= 1;
   void* args[] = {&z, &wpart, &nparts, &abs2, &nb2, &tv, &counter, &hist_row, &inv, &stop, &stop_on_purity, &t,
-                  &ncol, &nrow, &dX, &dP, &dXdP, &ts, &tk, &ti, &tc, &nterms, &nslots, &nchunk};
-  return hjit_on(h, h->k_final_rot, dim3((nterms + 2) * nchunk), dim3(128), args, st ? st : h->st);
+                  &ncol, &nrow, &dX, &dP, &dXdP, &ts, &tk, &ti, &tc, &nterms, &nslots, &nchunk, &prm, &np, &hstride};
+  return hjit_on(h, h->k_final_rot, dim3((nterms + 2) * nchunk, h->vc), dim3(128), args, st ? st : h->st);
 }
 
-static int ensure_hist(aw_state_s* h, long long rows) {
-  h->hist_cols = h->cfg.n_slots + 2;
-  const size_t need = (size_t)std::max(rows, 1LL) * h->hist_cols * 8;
+// room for `rows` observable rows of `cols` values per instance (cols 0: n_slots + 2)
+static int ensure_hist(aw_state_s* h, long long rows, int cols = 0) {
+  h->hist_cols = cols ? cols : h->cfg.n_slots + 2;
+  h->hist_cap = std::max(rows, 1LL);
+  const size_t need = (size_t)h->ni * h->hist_cap * h->hist_cols * 8;
   if (h->hist.bytes < need) TRY(dalloc(h->hist, need));
   h->hist_rows = 0;
-  h->hist_cap = rows;
+  return AW_OK;
+}
+
+// stop flags of the view at the start of a run: inactive instances stay stopped
+static int reset_stops(aw_state_s* h) {
+  std::vector<int> f(h->vc);
+  for (int k = 0; k < h->vc; ++k) f[k] = h->active.empty() || h->active[h->v0 + k] ? 0 : 1;
+  CK(cudaMemcpyAsync(dstop(h, h->v0), f.data(), f.size() * sizeof(int), cudaMemcpyHostToDevice, h->st));
   return AW_OK;
 }
 
 // normalize_rho_wigner (wigner_moyal_cuda_1d.py:608-622): W = rho2wigner(rho); norm; W, rho /= norm
-static int wm_normalize(aw_state_s* h, double* hist_row) {
-  WignerGrid g{h->W.p, h->nr, h->nc, &h->tw_r, &h->tw_c};
-  TRY(wigner_passes(h, g, h->rho.p, fsign(), false, true, true));
-  TRY(launch_finalize(h, 0.0, hist_row, 0));
-  TRY(settle(h));
-  KL(aw_k_scale(h->W.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
-  KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
+// (one instance at a time: the reducing Wigner transform feeds the single-instance finalize)
+static int wm_normalize(aw_state_s* h, long long hist_row) {
+  const int v0 = h->v0, vc = h->vc;
+  for (int i = v0; i < v0 + vc; ++i) {
+    h->v0 = i;
+    h->vc = 1;
+    WignerGrid g{h->W.p, h->nr, h->nc, &h->tw_r, &h->tw_c};
+    int r = wigner_passes(h, g, h->rho.p, fsign(), false, true, true);
+    if (!r) r = launch_finalize(h, 0.0, hist_of(h, i) + (size_t)hist_row * h->hist_cols, 0);
+    if (!r) r = settle(h);
+    if (!r) r = vscale(h, h->W.p, gsz(h));
+    if (!r) r = vscale(h, h->rho.p, gsz(h));
+    h->v0 = v0;
+    h->vc = vc;
+    TRY(r);
+  }
   return AW_OK;
 }
 
 extern "C" int aw_wigner2rho(aw_handle h) {
   if (!h) return fail(AW_E_ARG, "null handle");
   Settled guard{h};
+  TRY(clear_stops(h));
   if (!h->kn.rotated) return fail(AW_E_STATE, "wigner2rho exists for the Wigner-Moyal / Wigner-Bloch propagators");
   return wm_wigner2rho(h);
 }
@@ -1202,9 +1421,10 @@ extern "C" int aw_wigner2rho(aw_handle h) {
 extern "C" int aw_normalize_rho_wigner(aw_handle h) {
   if (!h) return fail(AW_E_ARG, "null handle");
   Settled guard{h};
+  TRY(clear_stops(h));
   if (!h->kn.rotated) return fail(AW_E_STATE, "normalize_rho_wigner exists for the Wigner-Moyal propagators");
   TRY(ensure_hist(h, 1));
-  return wm_normalize(h, (double*)h->hist.p);
+  return wm_normalize(h, 0);
 }
 
 static int vn_get_wigner(aw_state_s* h, int blackman);
@@ -1213,6 +1433,7 @@ static int sw_get_wigner(aw_state_s* h, int blackman);
 extern "C" int aw_rho2wigner(aw_handle h, int32_t blackman) {
   if (!h) return fail(AW_E_ARG, "null handle");
   Settled guard{h};
+  TRY(clear_stops(h));
   if (h->kn.rotated) {
     if (blackman) TRY(ensure_blackman(h, h->nr, h->nc));
     WignerGrid g{h->W.p, h->nr, h->nc, &h->tw_r, &h->tw_c};
@@ -1238,7 +1459,11 @@ struct StepPlan {
   bool ehrenfest;     // per-step Wigner transform, normalisation and observables
   bool keep_rho;      // write rho_n (position representation) every step
   int stop_on_purity; // Gibbs loop: stop after the first step with purity >= 1
+  bool per_inst = false;  // Bloch coefficients per instance (h->bvec) instead of dbeta, V_min, K_min
 };
+
+// Bloch coefficient vectors of a batch (ca = -dbeta/4 for V, -dbeta/2 for K; shift = minimum / 2)
+static double* bvec_of(aw_state_s* h, int which) { return (double*)h->bvec.p + (size_t)which * h->ni; }
 
 static AwFactor ftab(aw_state_s* h, int slot) {
   AwFactor f = fnone();
@@ -1252,6 +1477,9 @@ static int rot_tables_V(aw_state_s* h, const StepPlan& p, double tn, double tn1,
   const aw_config& c = h->cfg;
   if (p.bloch) {
     // bloch_expV: exp(-dbeta/4 (V(XX) + V(XX') - V_min)), split evenly over the two factors
+    if (p.per_inst)
+      return build_tab(h, TAB_BV, 0, 1, c.t_initial, 0.0, 0.0, 0.0, 0.0, 0, 0.0, nullptr, nullptr, 1, bvec_of(h, 0),
+                       bvec_of(h, 1));
     return build_tab(h, TAB_BV, 0, 1, c.t_initial, 0.0, -0.25 * p.dbeta, 0.0, 0.5 * h->V_min, 0, 0.0);
   }
   const double half = 0.5 * c.dt;
@@ -1262,6 +1490,9 @@ static int rot_tables_V(aw_state_s* h, const StepPlan& p, double tn, double tn1,
 
 static int rot_tables_K(aw_state_s* h, const StepPlan& p, double tn) {
   const aw_config& c = h->cfg;
+  if (p.bloch && p.per_inst)
+    return build_tab(h, TAB_BK, 1, 1, c.t_initial, 0.0, 0.0, 0.0, 0.0, 0, 0.0, nullptr, nullptr, 1, bvec_of(h, 2),
+                     bvec_of(h, 3));
   if (p.bloch)
     return build_tab(h, TAB_BK, 1, 1, c.t_initial, 0.0, -0.5 * p.dbeta, 0.0, 0.5 * h->K_min, 0, 0.0);
   return build_tab(h, TAB_K, 1, 0, tn + 0.5 * c.dt, 0.0, -c.dt, 0.0, 0.0, 0, 0.0);
@@ -1299,9 +1530,9 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
   // wait for the reduction, which runs on a side stream.  Bloch steps normalise every step.
   const bool defer = !p.bloch && p.ehrenfest && h->st2;
   // scale applied in the column pass: 1/N^2 and, for Bloch steps, 1/norm of the previous step
-  KL(aw_k_set2(dscal(h, 0), 1.0, 0.0, h->st));
-  CK(cudaMemsetAsync(h->stop.p, 0, sizeof(int), h->st));  // a stop raised by an earlier call must not persist
-  const int* stop = p.stop_on_purity ? (const int*)h->stop.p : nullptr;
+  TRY(vinv_reset(h));
+  TRY(reset_stops(h));  // a stop raised by an earlier call must not persist
+  const int* stop = p.stop_on_purity || h->ni > 1 ? (const int*)dstop(h) : nullptr;
 
   if (!vdep) TRY(rot_tables_V(h, p, times[1], times[1], false));
   if (!kdep) TRY(rot_tables_K(h, p, times[1]));
@@ -1354,7 +1585,7 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       a.in = a.out = h->rho.p;
       a.f0 = fnone();
       a.f0.scale = inv_n2;
-      a.f0.scale_ptr = p.ehrenfest && !defer ? dscal(h, 0) : nullptr;
+      a.f0.scale_ptr = p.ehrenfest && !defer ? dinv(h) : nullptr;
       a.f0.active = 1;
       a.d1 = -1;
       a.f1 = ftab(h, p.bloch ? TAB_BK : TAB_K);
@@ -1445,35 +1676,41 @@ extern "C" int aw_propagate(aw_handle h, int64_t steps, double* t) {
   for (long long n = 1; n <= steps + 1; ++n) times[n] = times[n - 1] + c.dt;  // self.t += self.dt
   TRY(ensure_hist(h, steps + 1));
   if (steps == 0) {
-    if (!c.ehrenfest) TRY(wm_normalize(h, (double*)h->hist.p));
+    if (!c.ehrenfest) TRY(wm_normalize(h, 0));
     return AW_OK;
   }
   StepPlan p{false, 0.0, c.ehrenfest != 0, false, 0};
-  TRY(rot_run(h, p, steps, times, (double*)h->hist.p));
+  TRY(rot_run(h, p, steps, times, hist_of(h, h->v0)));
   if (c.ehrenfest) {
     // the last step's normalisation, applied to both arrays
     TRY(settle(h));
-    KL(aw_k_scale(h->W.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
-    KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
+    TRY(vscale(h, h->W.p, gsz(h)));
+    TRY(vscale(h, h->rho.p, gsz(h)));
     h->hist_rows = steps;
   } else {
-    TRY(wm_normalize(h, (double*)h->hist.p + (size_t)steps * h->hist_cols));
+    TRY(wm_normalize(h, steps));
     h->hist_rows = 0;
   }
   *t = times[steps];
   return AW_OK;
 }
 
-extern "C" int aw_history(aw_handle h, double* out, int64_t max_rows, int64_t* rows, int32_t* cols) {
+extern "C" int aw_history_of(aw_handle h, int32_t inst, double* out, int64_t max_rows, int64_t* rows, int32_t* cols) {
   if (!h) return fail(AW_E_ARG, "null handle");
+  if (inst < 0 || inst >= h->ni) return fail(AW_E_ARG, "no instance %d", inst);
   const long long n = std::min<long long>(h->hist_rows, max_rows);
   if (rows) *rows = h->hist_rows;
   if (cols) *cols = h->hist_cols;
-  if (out && n > 0) {
-    CK(cudaMemcpyAsync(out, h->hist.p, (size_t)n * h->hist_cols * 8, cudaMemcpyDeviceToHost, h->st));
+  if (out && n > 0 && h->hist.p) {
+    CK(cudaMemcpyAsync(out, hist_of(h, inst), (size_t)n * h->hist_cols * 8, cudaMemcpyDeviceToHost, h->st));
   }
   CK(cudaStreamSynchronize(h->st));
   return AW_OK;
+}
+
+extern "C" int aw_history(aw_handle h, double* out, int64_t max_rows, int64_t* rows, int32_t* cols) {
+  if (!h) return fail(AW_E_ARG, "null handle");
+  return aw_history_of(h, h->v0, out, max_rows, rows, cols);
 }
 
 // ============================================================================ observables
@@ -1495,7 +1732,8 @@ extern "C" int aw_average(aw_handle h, const char* expr, double t, double* out) 
   if (h->kn.vn) return fail(AW_E_STATE, "use aw_average_ops for density-matrix propagators");
   cudaKernel_t k;
   TRY(get_obs_kernel(h, expr, &k));
-  const void* src = h->kn.rotated ? h->W.p : h->rho.p;
+  // the first instance of the view
+  const void* src = at_inst(h->kn.rotated ? h->W.p : h->rho.p, gsz(h), h->esz, h->v0);
   int f32 = h->f32, nr = h->kn.rotated ? h->nr : 1, nc = h->nc;
   double* part = (double*)h->part.p;
   double dX = h->cfg.dX, dP = h->cfg.dP;
@@ -1515,10 +1753,10 @@ extern "C" int aw_purity(aw_handle h, double* out) {
   if (!h || !out) return fail(AW_E_ARG, "null argument");
   double s[2];
   if (h->kn.rotated) {
-    TRY(dsum(h, h->W.p, (long long)h->nr * h->nc, 1, 0, s));
+    TRY(dsum(h, at_inst(h->W.p, gsz(h), h->esz, h->v0), gsz(h), 1, 0, s));
     *out = 2.0 * M_PI * s[0] * h->cfg.dXdP;
   } else if (h->kn.vn) {
-    TRY(dsum(h, h->rho.p, (long long)h->nr * h->nc, 2, 0, s));
+    TRY(dsum(h, at_inst(h->rho.p, gsz(h), h->esz, h->v0), gsz(h), 2, 0, s));
     *out = s[0] * h->cfg.dX * h->cfg.dX;
   } else {
     return fail(AW_E_STATE, "purity is defined for density-matrix and Wigner propagators");
@@ -1535,64 +1773,104 @@ extern "C" int aw_bloch_step(aw_handle h, double dbeta, double* out) {
   if (h->kind != AW_WIGNER_BLOCH) return fail(AW_E_STATE, "Bloch steps need a Bloch propagator");
   TRY(ensure_hist(h, 1));
   StepPlan p{true, dbeta, true, false, 0};
-  std::vector<double> times(3, 0.0);
-  TRY(rot_run(h, p, 1, times, (double*)h->hist.p));
-  TRY(settle(h));
-  KL(aw_k_scale(h->W.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
-  KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
-  if (out) {
-    CK(cudaMemcpyAsync(out, h->hist.p, (size_t)h->hist_cols * 8, cudaMemcpyDeviceToHost, h->st));
+  if (h->ni > 1) {
+    std::vector<double> db(h->vc, dbeta);
+    TRY(upload_bloch(h, db.data()));
+    p.per_inst = true;
   }
+  std::vector<double> times(3, 0.0);
+  TRY(rot_run(h, p, 1, times, hist_of(h, h->v0)));
+  TRY(settle(h));
+  TRY(vscale(h, h->W.p, gsz(h)));
+  TRY(vscale(h, h->rho.p, gsz(h)));
+  if (out) {
+    CK(cudaMemcpyAsync(out, hist_of(h, h->v0), (size_t)h->hist_cols * 8, cudaMemcpyDeviceToHost, h->st));
+  }
+  CK(cudaStreamSynchronize(h->st));
+  return AW_OK;
+}
+
+// get_gibbs_state's loop (wigner_bloch_cuda_1d.py:119-155) on every active instance of the view:
+// `steps` Bloch steps of dbeta[k], each instance stopping after its first step with purity >= 1;
+// done[k] / purity[k] report the steps that ran and the last purity.
+static int rot_gibbs(aw_state_s* h, const double* dbeta, long long steps, long long* done, double* purity) {
+  for (int k = 0; k < h->vc; ++k) {
+    if (done) done[k] = 0;
+  }
+  if (steps <= 0) return AW_OK;
+  TRY(ensure_hist(h, steps + 1));
+  CK(cudaMemsetAsync(h->hist.p, 0, (size_t)h->ni * h->hist_cap * h->hist_cols * 8, h->st));
+  TRY(dalloc(h->snap, (size_t)h->ni * gsz(h) * h->esz));
+  StepPlan p{true, dbeta[0], true, true, 1};
+  if (h->ni > 1) {
+    TRY(upload_bloch(h, dbeta));
+    p.per_inst = true;
+  }
+  std::vector<double> times(steps + 2, 0.0);
+  TRY(rot_run(h, p, steps, times, hist_of(h, h->v0)));
+  // how many steps ran: rows are written in order until the stop flag is raised; the finalize
+  // of the stopping step still writes (the flag is checked at entry), so count rows whose norm
+  // entry was written
+  const int cols = h->hist_cols;
+  std::vector<double> hh((size_t)h->vc * h->hist_cap * cols);
+  CK(cudaMemcpyAsync(hh.data(), hist_of(h, h->v0), hh.size() * 8, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  std::vector<long long> ran(h->vc, 0);
+  for (int k = 0; k < h->vc; ++k) {
+    const double* hk = hh.data() + (size_t)k * h->hist_cap * cols;
+    for (long long n = 0; n < steps; ++n) {
+      if (hk[(size_t)n * cols + cols - 1] == 0.0) break;
+      ran[k] = n + 1;
+    }
+    if (done) done[k] = ran[k];
+    if (purity && ran[k] > 0) purity[k] = hk[(size_t)(ran[k] - 1) * cols + cols - 2];
+  }
+  // rho_n of the last executed step (position representation, unnormalised) and its W, for the
+  // instances that ran
+  TRY(settle(h));
+  TRY(reset_stops(h));
+  for (int k = 0; k < h->vc; ++k) {
+    const int i = h->v0 + k;
+    if (ran[k] == 0) continue;
+    CK(cudaMemcpyAsync(at_inst(h->rho.p, gsz(h), h->esz, i), at_inst(h->snap.p, gsz(h), h->esz, i),
+                       (size_t)gsz(h) * h->esz, cudaMemcpyDeviceToDevice, h->st));
+  }
+  {
+    WignerGrid g{h->W.p, h->nr, h->nc, &h->tw_r, &h->tw_c};
+    TRY(wigner_passes(h, g, h->rho.p, fsign(), false, false, true));
+  }
+  TRY(settle(h));
+  TRY(vscale(h, h->W.p, gsz(h)));
+  TRY(vscale(h, h->rho.p, gsz(h)));
   CK(cudaStreamSynchronize(h->st));
   return AW_OK;
 }
 
 extern "C" int aw_gibbs(aw_handle h, double dbeta, int64_t steps, int64_t* done, double* purity) {
   if (!h) return fail(AW_E_ARG, "null handle");
+  std::vector<double> db(h->vc, dbeta);
+  std::vector<int64_t> d(h->vc, 0);
+  std::vector<double> pu(h->vc, 0.0);
+  TRY(aw_gibbs_batch(h, db.data(), steps, d.data(), pu.data()));
+  if (done) *done = d[0];
+  if (purity && d[0] > 0) *purity = pu[0];
+  return AW_OK;
+}
+
+extern "C" int aw_gibbs_batch(aw_handle h, const double* dbeta, int64_t steps, int64_t* done, double* purity) {
+  if (!h || !dbeta) return fail(AW_E_ARG, "null argument");
   Settled guard{h};
-  int vn_gibbs(aw_state_s*, double, long long, long long*, double*);
+  int vn_gibbs(aw_state_s*, const double*, long long, long long*, double*);
+  std::vector<long long> d(h->vc, 0);
   if (h->kind == AW_RHO_BLOCH) {
-    long long d = 0;
-    TRY(vn_gibbs(h, dbeta, steps, &d, purity));
-    if (done) *done = d;
-    return AW_OK;
+    TRY(vn_gibbs(h, dbeta, steps, d.data(), purity));
+  } else if (h->kind == AW_WIGNER_BLOCH) {
+    TRY(rot_gibbs(h, dbeta, steps, d.data(), purity));
+  } else {
+    return fail(AW_E_STATE, "get_gibbs_state needs a Bloch propagator");
   }
-  if (h->kind != AW_WIGNER_BLOCH) return fail(AW_E_STATE, "get_gibbs_state needs a Bloch propagator");
-  if (steps <= 0) {
-    if (done) *done = 0;
-    return AW_OK;
-  }
-  TRY(ensure_hist(h, steps + 1));
-  CK(cudaMemsetAsync(h->hist.p, 0, (size_t)(steps + 1) * h->hist_cols * 8, h->st));
-  TRY(dalloc(h->snap, (size_t)h->nr * h->nc * h->esz));
-  StepPlan p{true, dbeta, true, true, 1};
-  std::vector<double> times(steps + 2, 0.0);
-  TRY(rot_run(h, p, steps, times, (double*)h->hist.p));
-  // how many steps ran: rows with a non-zero norm
-  std::vector<double> hh((size_t)steps * h->hist_cols);
-  CK(cudaMemcpyAsync(hh.data(), h->hist.p, hh.size() * 8, cudaMemcpyDeviceToHost, h->st));
-  CK(cudaStreamSynchronize(h->st));
-  long long ran = 0;
-  const int cols = h->hist_cols;
-  // rows are written in order until the stop flag is raised; the finalize of the stopping step still writes
-  // (the flag is checked at entry), so count rows whose norm entry was written
-  for (long long n = 0; n < steps; ++n) {
-    if (hh[(size_t)n * cols + cols - 1] == 0.0) break;
-    ran = n + 1;
-  }
-  if (done) *done = ran;
-  if (purity && ran > 0) *purity = hh[(size_t)(ran - 1) * cols + cols - 2];
-  // rho_n of the last executed step (position representation, unnormalised) and its W
-  TRY(settle(h));
-  CK(cudaMemcpyAsync(h->rho.p, h->snap.p, (size_t)h->nr * h->nc * h->esz, cudaMemcpyDeviceToDevice, h->st));
-  {
-    WignerGrid g{h->W.p, h->nr, h->nc, &h->tw_r, &h->tw_c};
-    TRY(wigner_passes(h, g, h->rho.p, fsign(), false, false, true));
-  }
-  TRY(settle(h));
-  KL(aw_k_scale(h->W.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
-  KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
-  CK(cudaStreamSynchronize(h->st));
+  if (done)
+    for (int k = 0; k < h->vc; ++k) done[k] = d[k];
   return AW_OK;
 }
 
@@ -1607,10 +1885,17 @@ struct VnPlan {
   bool keep_rho;       // store rho_n (position representation) every step
   int stop_on_purity;
   int complex_trace;   // rho-Bloch divides by the complex trace (rho_bloch_cuda_1d.py:244)
+  bool per_inst = false;  // Bloch coefficients per instance (h->bvec)
 };
 
 static int vn_tables(aw_state_s* h, const VnPlan& p, double tn, bool kfirst) {
   const aw_config& c = h->cfg;
+  if (p.bloch && p.per_inst) {
+    TRY(build_tab(h, TAB_BV, 0, 1, c.t_initial, 0.0, 0.0, 0.0, 0.0, 0, 0.0, nullptr, nullptr, 1, bvec_of(h, 0),
+                  bvec_of(h, 1)));
+    return build_tab(h, TAB_BK, 1, 1, c.t_initial, 0.0, 0.0, 0.0, 0.0, 0, 0.0, nullptr, nullptr, 1, bvec_of(h, 2),
+                     bvec_of(h, 3));
+  }
   if (p.bloch) {
     TRY(build_tab(h, TAB_BV, 0, 1, c.t_initial, 0.0, -0.25 * p.dbeta, 0.0, 0.5 * h->V_min, 0, 0.0));
     return build_tab(h, TAB_BK, 1, 1, c.t_initial, 0.0, -0.5 * p.dbeta, 0.0, 0.5 * h->K_min, 0, 0.0);
@@ -1625,15 +1910,17 @@ static int vn_tables(aw_state_s* h, const VnPlan& p, double tn, bool kfirst) {
 
 // momentum-space diagonal of rho_n:  M_k = (1/N) Sum_i [fft1(S rho_n)]_ik exp(+2 pi i k i / N),
 // so that Tr[g(p) rho] dX = Sum_k g(P_k) M_k dX (the p branch of get_average, vn:548-561)
+//   hist: the first instance's rows (hist_stride values apart), instances inst_stride values apart
 static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::vector<double>& times, double* hist,
-                  int hist_stride) {
+                  int hist_stride, long long inst_stride = 0) {
   const aw_config& c = h->cfg;
   const bool vdep = !p.bloch && c.v_time_dependent;
   const bool kdep = !p.bloch && c.k_time_dependent;
   const int N = h->nc;
-  KL(aw_k_set2(dscal(h, 0), 1.0, 0.0, h->st));
-  CK(cudaMemsetAsync(h->stop.p, 0, sizeof(int), h->st));  // a stop raised by an earlier call must not persist
-  const int* stop = p.stop_on_purity ? (const int*)h->stop.p : nullptr;
+  if (h->ni > 1 && p.observables) return fail(AW_E_STATE, "per-step observables need a single propagator");
+  TRY(vinv_reset(h));
+  TRY(reset_stops(h));  // a stop raised by an earlier call must not persist
+  const int* stop = p.stop_on_purity || h->ni > 1 ? (const int*)dstop(h) : nullptr;
   const int row_blocks = aw_row_pass_blocks(h->nr, h->nc, h->f32);
   const int vslot = p.bloch ? TAB_BV : TAB_V1;
   const int kslot = p.bloch ? TAB_BK : TAB_K;
@@ -1656,7 +1943,7 @@ static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::ve
       AwPassArgs a = pnone(h);
       a.in = a.out = h->rho.p;
       a.f0 = fnone();
-      a.f0.scale_ptr = dscal(h, 0);
+      a.f0.scale_ptr = dinv(h);
       a.f0.active = 1;
       a.d1 = -1;
       a.f1 = ftab(h, kslot);
@@ -1709,13 +1996,14 @@ static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::ve
       TRY(col_pass(h, a, h->tw_c));
     }
     if (p.bloch || !p.observables) {
-      KL(aw_k_trace_finalize((const double2*)h->diag.p, N, (const double*)h->abs2.p, row_blocks, c.dX,
-                             p.complex_trace, dscal(h, 0), p.observables ? nullptr : hrow, (int*)h->stop.p,
-                             p.stop_on_purity, h->st));
+      KL(aw_k_trace_finalize_n((const double2*)h->diag.p + (size_t)h->v0 * N,
+                               N, (const double*)h->abs2.p + (size_t)h->v0 * row_blocks, row_blocks, c.dX,
+                               p.complex_trace, dinv(h, h->v0), p.observables ? nullptr : hrow, inst_stride,
+                               dstop(h, h->v0), p.stop_on_purity, h->vc, h->st));
     }
     if (p.observables) {
       FinalArgs f{(const double*)h->diag.p, 2, N, (const double*)h->red_line.p, 1, N, 0, nullptr, c.dX,
-                  p.bloch ? nullptr : dscal(h, 0), 0, 0};
+                  p.bloch ? nullptr : dinv(h), 0, 0};
       TRY(launch_finalize_args(h, f, times[n], hrow, 0));
     }
   }
@@ -1730,15 +2018,16 @@ int vn_propagate(aw_state_s* h, long long steps, double* t) {
   TRY(ensure_hist(h, steps + 1));
   if (steps == 0) return AW_OK;
   VnPlan p{false, 0.0, c.ehrenfest != 0, false, 0, 0};
-  TRY(vn_run(h, p, steps, times, c.ehrenfest ? (double*)h->hist.p : nullptr, h->hist_cols));
+  TRY(vn_run(h, p, steps, times, c.ehrenfest ? hist_of(h, h->v0) : nullptr, h->hist_cols));
   TRY(settle(h));
-  KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
+  TRY(vscale(h, h->rho.p, gsz(h)));
   h->hist_rows = c.ehrenfest ? steps : 0;
   *t = times[steps];
   return AW_OK;
 }
 
 int vn_bloch_step(aw_state_s* h, double dbeta, double* out) {
+  if (h->ni > 1) return fail(AW_E_STATE, "single rho-Bloch steps need a single propagator (use aw_gibbs_batch)");
   TRY(ensure_hist(h, 2));
   CK(cudaMemsetAsync(h->hist.p, 0, 2 * (size_t)h->hist_cols * 8, h->st));
   const bool obs = h->cfg.n_slots > 0;
@@ -1748,10 +2037,10 @@ int vn_bloch_step(aw_state_s* h, double dbeta, double* out) {
   TRY(vn_run(h, p, 1, times, (double*)h->hist.p, h->hist_cols));
   if (obs)
     KL(aw_k_trace_finalize((const double2*)h->diag.p, h->nc, (const double*)h->abs2.p,
-                           aw_row_pass_blocks(h->nr, h->nc, h->f32), h->cfg.dX, 1, dscal(h, 2),
+                           aw_row_pass_blocks(h->nr, h->nc, h->f32), h->cfg.dX, 1, dmisc(h, 0),
                            (double*)h->hist.p + h->hist_cols, nullptr, 0, h->st));
   TRY(settle(h));
-  KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
+  TRY(vscale(h, h->rho.p, gsz(h)));
   if (out) {
     std::vector<double> hh(2 * (size_t)h->hist_cols);
     CK(cudaMemcpyAsync(hh.data(), h->hist.p, hh.size() * 8, cudaMemcpyDeviceToHost, h->st));
@@ -1765,30 +2054,41 @@ int vn_bloch_step(aw_state_s* h, double dbeta, double* out) {
   return AW_OK;
 }
 
-int vn_gibbs(aw_state_s* h, double dbeta, long long steps, long long* done, double* purity) {
-  *done = 0;
+int vn_gibbs(aw_state_s* h, const double* dbeta, long long steps, long long* done, double* purity) {
+  for (int k = 0; k < h->vc; ++k) done[k] = 0;
   if (steps <= 0) return AW_OK;
-  TRY(ensure_hist(h, steps + 1));
-  const int hc = 3;
-  TRY(dalloc(h->hist, (size_t)(steps + 1) * hc * 8));
-  CK(cudaMemsetAsync(h->hist.p, 0, (size_t)(steps + 1) * hc * 8, h->st));
-  TRY(dalloc(h->snap, (size_t)h->nr * h->nc * h->esz));
-  VnPlan p{true, dbeta, false, true, 1, 1};
-  std::vector<double> times(steps + 2, 0.0);
-  TRY(vn_run(h, p, steps, times, (double*)h->hist.p, hc));
-  std::vector<double> hh((size_t)steps * hc);
-  CK(cudaMemcpyAsync(hh.data(), h->hist.p, hh.size() * 8, cudaMemcpyDeviceToHost, h->st));
-  CK(cudaStreamSynchronize(h->st));
-  long long ran = 0;
-  for (long long n = 0; n < steps; ++n) {
-    if (hh[(size_t)n * hc + 1] == 0.0) break;
-    ran = n + 1;
+  const int hc = 3;  // purity, Re trace, Im trace
+  TRY(ensure_hist(h, steps + 1, hc));
+  CK(cudaMemsetAsync(h->hist.p, 0, (size_t)h->ni * h->hist_cap * hc * 8, h->st));
+  TRY(dalloc(h->snap, (size_t)h->ni * gsz(h) * h->esz));
+  VnPlan p{true, dbeta[0], false, true, 1, 1};
+  if (h->ni > 1) {
+    TRY(upload_bloch(h, dbeta));
+    p.per_inst = true;
   }
-  *done = ran;
-  if (purity && ran > 0) *purity = hh[(size_t)(ran - 1) * hc];
+  std::vector<double> times(steps + 2, 0.0);
+  TRY(vn_run(h, p, steps, times, hist_of(h, h->v0), hc, h->hist_cap * hc));
+  std::vector<double> hh((size_t)h->vc * h->hist_cap * hc);
+  CK(cudaMemcpyAsync(hh.data(), hist_of(h, h->v0), hh.size() * 8, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  std::vector<long long> ran(h->vc, 0);
+  for (int k = 0; k < h->vc; ++k) {
+    const double* hk = hh.data() + (size_t)k * h->hist_cap * hc;
+    for (long long n = 0; n < steps; ++n) {
+      if (hk[(size_t)n * hc + 1] == 0.0) break;
+      ran[k] = n + 1;
+    }
+    done[k] = ran[k];
+    if (purity && ran[k] > 0) purity[k] = hk[(size_t)(ran[k] - 1) * hc];
+  }
   TRY(settle(h));
-  CK(cudaMemcpyAsync(h->rho.p, h->snap.p, (size_t)h->nr * h->nc * h->esz, cudaMemcpyDeviceToDevice, h->st));
-  KL(aw_k_scale(h->rho.p, h->f32, (long long)h->nr * h->nc, 1.0, 0.0, dscal(h, 0), h->st));
+  for (int k = 0; k < h->vc; ++k) {
+    const int i = h->v0 + k;
+    if (ran[k] == 0) continue;
+    CK(cudaMemcpyAsync(at_inst(h->rho.p, gsz(h), h->esz, i), at_inst(h->snap.p, gsz(h), h->esz, i),
+                       (size_t)gsz(h) * h->esz, cudaMemcpyDeviceToDevice, h->st));
+  }
+  TRY(vscale(h, h->rho.p, gsz(h)));
   CK(cudaStreamSynchronize(h->st));
   h->hist_rows = 0;
   return AW_OK;
@@ -1798,14 +2098,36 @@ int vn_gibbs(aw_state_s* h, double dbeta, long long steps, long long* done, doub
 // (2N)^2 grid, sign flip, three shears, ifft0, sign flip, normalise by Re Sum W dXdP_wigner
 static int vn_get_wigner(aw_state_s* h, int blackman) {
   const int N = h->nc, M = h->wn, pad = N / 2;
-  KL(aw_k_embed(h->rho.p, h->f32, N, h->W.p, M, pad, h->st));
   if (blackman) TRY(ensure_blackman(h, M, M));
-  WignerGrid g{h->W.p, M, M, &h->tw_w, &h->tw_w};
-  TRY(wigner_passes(h, g, h->W.p, fsign(), blackman != 0, false, true));
-  TRY(settle(h));
-  double s[2];
-  TRY(dsum(h, h->W.p, (long long)M * M, 0, 0, s));
-  KL(aw_k_scale(h->W.p, h->f32, (long long)M * M, 1.0 / (s[0] * h->cfg.dXdP), 0.0, nullptr, h->st));
+  const int v0 = h->v0, vc = h->vc;
+  for (int i = v0; i < v0 + vc; ++i) {
+    h->v0 = i;
+    h->vc = 1;
+    void* Wi = at_inst(h->W.p, (long long)M * M, h->esz, i);
+    int r = 0;
+    {
+      cudaEvent_t pe_ = prof_mark(h);
+      r = aw_k_embed(at_inst(h->rho.p, gsz(h), h->esz, i), h->f32, N, Wi, M, pad, h->st);
+      prof_done(h, PROF_UTIL, 0.0, pe_);
+      ++g_launches;
+      if (r) r = fail(AW_E_CUDA, "embedding launch failed");
+    }
+    WignerGrid g{h->W.p, M, M, &h->tw_w, &h->tw_w};
+    if (!r) r = wigner_passes(h, g, h->W.p, fsign(), blackman != 0, false, true);
+    if (!r) r = settle(h);
+    double sm[2] = {0.0, 0.0};
+    if (!r) r = dsum(h, Wi, (long long)M * M, 0, 0, sm);
+    if (!r) {
+      cudaEvent_t pe_ = prof_mark(h);
+      r = aw_k_scale(Wi, h->f32, (long long)M * M, 1.0 / (sm[0] * h->cfg.dXdP), 0.0, nullptr, h->st);
+      prof_done(h, PROF_UTIL, 0.0, pe_);
+      ++g_launches;
+      if (r) r = fail(AW_E_CUDA, "scale launch failed");
+    }
+    h->v0 = v0;
+    h->vc = vc;
+    TRY(r);
+  }
   return AW_OK;
 }
 
@@ -1814,7 +2136,20 @@ extern "C" int aw_average_ops(aw_handle h, const char* const* ops, int32_t n_ops
   if (!h->kn.vn) return fail(AW_E_STATE, "ordered operator averages are defined for density matrices");
   Settled guard{h};
   const long long n = (long long)h->nr * h->nc;
-  CK(cudaMemcpyAsync(h->tmp.p, h->rho.p, n * h->esz, cudaMemcpyDeviceToDevice, h->st));
+  const int keep_v0 = h->v0, keep_vc = h->vc;
+  // the first instance of the view, copied to the scratch buffer (which the passes treat as instance 0)
+  CK(cudaMemcpyAsync(h->tmp.p, at_inst(h->rho.p, n, h->esz, h->v0), n * h->esz, cudaMemcpyDeviceToDevice, h->st));
+  h->v0 = 0;
+  h->vc = 1;
+  struct ViewBack {
+    aw_state_s* h;
+    int v0, vc;
+    ~ViewBack() {
+      h->v0 = v0;
+      h->vc = vc;
+    }
+  } view_back{h, keep_v0, keep_vc};
+  TRY(clear_stops(h));
   bool is_x = false;
   for (int k = 0; k < n_ops; ++k) {
     is_x = !is_x;
@@ -1878,7 +2213,7 @@ static int sw_finalize(aw_state_s* h, double t, double* hrow) {
   double* pmar = (double*)h->red_cross.p; // |(fft psi)_k|^2
   KL(aw_k_abs2(h->W.p, h->f32, N, xm, h->st));
   KL(aw_k_abs2(h->tmp.p, h->f32, N, pmar, h->st));
-  FinalArgs f{xm, 1, N, pmar, 1, N, N / 2, nullptr, h->cfg.dX, dscal(h, 0), 1, 1};
+  FinalArgs f{xm, 1, N, pmar, 1, N, N / 2, nullptr, h->cfg.dX, dinv(h), 1, 1};
   return launch_finalize_args(h, f, t, hrow, 0);
 }
 
@@ -1890,7 +2225,7 @@ int sw_propagate(aw_state_s* h, long long steps, double* t) {
   TRY(ensure_hist(h, steps + 1));
   if (steps == 0) return AW_OK;
   const bool tdep = c.v_time_dependent || c.k_time_dependent || c.absx_mode == 2 || c.absp_mode == 2;
-  KL(aw_k_set2(dscal(h, 0), 1.0, 0.0, h->st));
+  KL(aw_k_set2(dinv(h), 1.0, 0.0, h->st));
   if (!tdep) TRY(sw_tables(h, times[1]));
   const int nb = aw_row_pass_blocks(h->sw_rows, h->nc, h->f32);
   for (long long n = 1; n <= steps; ++n) {
@@ -1900,7 +2235,7 @@ int sw_propagate(aw_state_s* h, long long steps, double* t) {
     a.out = c.ehrenfest ? h->W.p : h->rho.p;
     a.f0 = ftab(h, TAB_V1);
     a.f0.row_tab = nullptr;
-    a.f0.scale_ptr = dscal(h, 0);
+    a.f0.scale_ptr = dinv(h);
     a.d1 = +1;
     a.f1 = ftab(h, TAB_K);
     a.f1.row_tab = nullptr;
@@ -1924,10 +2259,10 @@ int sw_propagate(aw_state_s* h, long long steps, double* t) {
       TRY(sw_finalize(h, times[n], (double*)h->hist.p + (size_t)(n - 1) * h->hist_cols));
       CK(cudaMemcpyAsync(h->rho.p, h->W.p, (size_t)h->sw_rows * h->nc * h->esz, cudaMemcpyDeviceToDevice, h->st));
     } else {
-      KL(aw_k_norm_finalize((const double*)h->abs2.p, nb, c.dX, dscal(h, 0), nullptr, h->st));
+      KL(aw_k_norm_finalize((const double*)h->abs2.p, nb, c.dX, dinv(h), nullptr, h->st));
     }
   }
-  KL(aw_k_scale(h->rho.p, h->f32, h->nc, 1.0, 0.0, dscal(h, 0), h->st));
+  KL(aw_k_scale(h->rho.p, h->f32, h->nc, 1.0, 0.0, dinv(h), h->st));
   h->hist_rows = c.ehrenfest ? steps : 0;
   *t = times[steps];
   return AW_OK;
@@ -2007,8 +2342,8 @@ extern "C" int aw_sw_imag_steps(aw_handle h, int64_t steps, int32_t project) {
     TRY(row_pass(h, a, h->tw_r));
     if (!project) {
       // psi /= norm(psi) sqrt(dX)
-      KL(aw_k_norm_finalize((const double*)h->abs2.p, nb, c.dX, dscal(h, 0), nullptr, h->st));
-      KL(aw_k_scale(h->rho.p, h->f32, N, 1.0, 0.0, dscal(h, 0), h->st));
+      KL(aw_k_norm_finalize((const double*)h->abs2.p, nb, c.dX, dinv(h), nullptr, h->st));
+      KL(aw_k_scale(h->rho.p, h->f32, N, 1.0, 0.0, dinv(h), h->st));
     } else {
       // projectout_stationary_states (sw:505-550): normalise, subtract projections, normalise
       double s[2];
@@ -2092,5 +2427,87 @@ extern "C" int aw_sw_energy(aw_handle h, double t, double* out) {
   k = 0;
   for (double x : hp) k += x;
   *out = v / n1[0] + k / n2[0];
+  return AW_OK;
+}
+
+// ============================================================================ batches
+// Independent instances of one propagator kind and grid, stepped together: every pass launch
+// covers the view's instances (blockIdx.y), each with its own state, tables, parameters, norm,
+// stop flag and observable rows; no instance reads another's data, so an instance's results do
+// not depend on which others share the batch.
+static int clear_stops(aw_state_s* h) {
+  CK(cudaMemsetAsync(dstop(h, h->v0), 0, (size_t)h->vc * sizeof(int), h->st));
+  return AW_OK;
+}
+
+extern "C" int aw_set_view(aw_handle h, int32_t first, int32_t count) {
+  if (!h) return fail(AW_E_ARG, "null handle");
+  if (first < 0 || count < 1 || first + count > h->ni)
+    return fail(AW_E_ARG, "view [%d, %d) outside the %d instances", first, first + count, h->ni);
+  TRY(settle(h));
+  h->v0 = first;
+  h->vc = count;
+  return AW_OK;
+}
+
+extern "C" int aw_set_params(aw_handle h, int32_t inst, const double* values) {
+  if (!h || (!values && h->np)) return fail(AW_E_ARG, "null argument");
+  if (inst < 0 || inst >= h->ni) return fail(AW_E_ARG, "no instance %d", inst);
+  if (!h->np) return AW_OK;
+  CK(cudaMemcpyAsync((double*)h->params.p + (size_t)inst * h->np, values, (size_t)h->np * sizeof(double),
+                     cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->minima_ok[inst] = 0;
+  h->maskx_ready = h->maskp_ready = false;  // masks may depend on the parameters
+  return AW_OK;
+}
+
+extern "C" int aw_set_active(aw_handle h, const int32_t* flags) {
+  if (!h || !flags) return fail(AW_E_ARG, "null argument");
+  for (int i = 0; i < h->ni; ++i) h->active[i] = flags[i] != 0;
+  return AW_OK;
+}
+
+extern "C" int aw_bloch_min_of(aw_handle h, int32_t inst, double* v_min, double* k_min) {
+  if (!h) return fail(AW_E_ARG, "null handle");
+  if (inst < 0 || inst >= h->ni) return fail(AW_E_ARG, "no instance %d", inst);
+  if (h->kind != AW_WIGNER_BLOCH && h->kind != AW_RHO_BLOCH) return fail(AW_E_STATE, "minima exist for Bloch propagators");
+  if (!h->minima_ok[inst]) TRY(bloch_minima(h, inst));
+  if (v_min) *v_min = h->vmin_i[inst];
+  if (k_min) *k_min = h->kmin_i[inst];
+  return AW_OK;
+}
+
+extern "C" int aw_init_state(aw_handle h) {
+  if (!h) return fail(AW_E_ARG, "null handle");
+  if (!h->k_binit) return fail(AW_E_STATE, "the handle was created without init_expr");
+  if (h->kn.sw) return fail(AW_E_STATE, "aw_init_state exists for the grid propagators");
+  Settled guard{h};
+  const long long n = gsz(h);
+  void* dst = h->kn.rotated ? h->W.p : h->rho.p;
+  for (int i = h->v0; i < h->v0 + h->vc; ++i) {
+    void* out = at_inst(dst, n, h->esz, i);
+    int f32 = h->f32, nr = h->nr, nc = h->nc;
+    double da = h->cfg.dX, db = h->kn.rotated ? h->cfg.dP : h->cfg.dX;
+    const double* prm = h->np ? (const double*)h->params.p + (size_t)i * h->np : nullptr;
+    void* args[] = {&out, &f32, &nr, &nc, &da, &db, &prm};
+    TRY(hjit(h, h->k_binit, dim3((nc + 127) / 128, nr), dim3(128), args));
+    double s[2];
+    if (h->kn.rotated) {
+      // set_wignerfunction: W /= Sum W dXdP (complex, wigner_moyal_cuda_1d.py:415)
+      TRY(dsum(h, out, n, 0, 0, s));
+      const double d = (s[0] * s[0] + s[1] * s[1]) * h->cfg.dXdP;
+      KL(aw_k_scale(out, h->f32, n, s[0] / d, -s[1] / d, nullptr, h->st));
+    } else {
+      // set_rho: rho /= Re Tr(rho) dX (rho_vneumann_cuda_1d.py:382-384)
+      TRY(dsum(h, out, h->nr, 3, h->nc + 1, s));
+      KL(aw_k_scale(out, h->f32, n, 1.0 / (s[0] * h->cfg.dX), 0.0, nullptr, h->st));
+    }
+  }
+  if (h->kn.rotated) {
+    TRY(clear_stops(h));
+    TRY(wm_wigner2rho(h));
+  }
+  CK(cudaStreamSynchronize(h->st));
   return AW_OK;
 }

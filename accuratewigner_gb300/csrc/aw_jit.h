@@ -105,34 +105,65 @@ struct KindNames {
   bool sw;          // SW: 1-D wave function
 };
 
+// Per-instance parameters (batched propagators): each name becomes a macro that reads the
+// instance's row of the parameter table, through the aw_prm argument that every function of a
+// user expression takes (null for a single propagator, whose constants are #defines).
+inline std::string param_macros(const std::vector<std::string>& params) {
+  std::string s;
+  for (size_t k = 0; k < params.size(); ++k)
+    s += "#define " + params[k] + " (aw_prm[" + std::to_string(k) + "])\n";
+  return s;
+}
+
 inline std::string module_source(const KindNames& kn, const std::string& consts, const std::string& V,
                                  const std::string& K, const std::string& absx, const std::string& absp,
-                                 const std::vector<std::string>& obs_x, const std::vector<std::string>& obs_p) {
+                                 const std::vector<std::string>& obs_x, const std::vector<std::string>& obs_p,
+                                 const std::vector<std::string>& params = {}, const std::string& init = "") {
   std::string s = prelude();
   s += "\n// ---- user constants and functions\n";
   s += consts;
+  s += "\n";
+  s += param_macros(params);
   s += "\n// ---- energies (wigner_moyal_cuda_1d.py:723-733)\n";
-  s += "__device__ double K(double P, double t) { return (" + K + "); }\n";
-  s += "__device__ double V(double X, double t) { return (" + V + "); }\n";
+  s += "__device__ double K(double P, double t, const double* aw_prm) { return (" + K + "); }\n";
+  s += "__device__ double V(double X, double t, const double* aw_prm) { return (" + V + "); }\n";
   if (kn.rotated) {
-    s += "__device__ double aw_absx2d(aw_size_t i, aw_size_t j, double XX, double XX_prime, double PP, double PP_prime, double t) { return (" + absx + "); }\n";
-    s += "__device__ double aw_absp2d(aw_size_t i, aw_size_t j, double XX, double XX_prime, double PP, double PP_prime, double t) { return (" + absp + "); }\n";
-    s += "__device__ double aw_mask1(int aw_fn, aw_size_t j, double aw_x, double t) { return 1.0; }\n";
+    s += "__device__ double aw_absx2d(aw_size_t i, aw_size_t j, double XX, double XX_prime, double PP, double PP_prime, double t, const double* aw_prm) { return (" + absx + "); }\n";
+    s += "__device__ double aw_absp2d(aw_size_t i, aw_size_t j, double XX, double XX_prime, double PP, double PP_prime, double t, const double* aw_prm) { return (" + absp + "); }\n";
+    s += "__device__ double aw_mask1(int aw_fn, aw_size_t j, double aw_x, double t, const double* aw_prm) { return 1.0; }\n";
   } else if (kn.vn) {
-    s += "__device__ double abs_boundary_x(double X) { return (" + absx + "); }\n";
-    s += "__device__ double abs_boundary_p(double P) { return (" + absp + "); }\n";
-    s += "__device__ double aw_mask1(int aw_fn, aw_size_t j, double aw_x, double t) { return aw_fn == 0 ? abs_boundary_x(aw_x) : abs_boundary_p(aw_x); }\n";
+    s += "__device__ double abs_boundary_x(double X, const double* aw_prm) { return (" + absx + "); }\n";
+    s += "__device__ double abs_boundary_p(double P, const double* aw_prm) { return (" + absp + "); }\n";
+    s += "__device__ double aw_mask1(int aw_fn, aw_size_t j, double aw_x, double t, const double* aw_prm) { return aw_fn == 0 ? abs_boundary_x(aw_x, aw_prm) : abs_boundary_p(aw_x, aw_prm); }\n";
   } else {
-    s += "__device__ double aw_absx1(aw_size_t j, double X, double t) { return (" + absx + "); }\n";
-    s += "__device__ double aw_absp1(aw_size_t j, double P, double t) { return (" + absp + "); }\n";
-    s += "__device__ double aw_mask1(int aw_fn, aw_size_t j, double aw_x, double t) { return aw_fn == 0 ? aw_absx1(j, aw_x, t) : aw_absp1(j, aw_x, t); }\n";
+    s += "__device__ double aw_absx1(aw_size_t j, double X, double t, const double* aw_prm) { return (" + absx + "); }\n";
+    s += "__device__ double aw_absp1(aw_size_t j, double P, double t, const double* aw_prm) { return (" + absp + "); }\n";
+    s += "__device__ double aw_mask1(int aw_fn, aw_size_t j, double aw_x, double t, const double* aw_prm) { return aw_fn == 0 ? aw_absx1(j, aw_x, t, aw_prm) : aw_absp1(j, aw_x, t, aw_prm); }\n";
   }
-  s += "__device__ double aw_obs_x(int aw_k, double X, double t) {\n  switch (aw_k) {\n";
+  s += "__device__ double aw_obs_x(int aw_k, double X, double t, const double* aw_prm) {\n  switch (aw_k) {\n";
   for (size_t k = 0; k < obs_x.size(); ++k) s += "    case " + std::to_string(k) + ": return (" + obs_x[k] + ");\n";
   s += "  }\n  return 0.0;\n}\n";
-  s += "__device__ double aw_obs_p(int aw_k, double P, double t) {\n  switch (aw_k) {\n";
+  s += "__device__ double aw_obs_p(int aw_k, double P, double t, const double* aw_prm) {\n  switch (aw_k) {\n";
   for (size_t k = 0; k < obs_p.size(); ++k) s += "    case " + std::to_string(k) + ": return (" + obs_p[k] + ");\n";
   s += "  }\n  return 0.0;\n}\n";
+  if (!init.empty()) {
+    // initial state of one instance of a batch: W(X, P) for the rotated frame, rho(X, X_prime) else
+    if (kn.rotated)
+      s += "__device__ cuda_complex aw_init_value(aw_size_t i, aw_size_t j, double X, double P, const double* aw_prm) { return cuda_complex(" + init + "); }\n";
+    else
+      s += "__device__ cuda_complex aw_init_value(aw_size_t i, aw_size_t j, double X, double X_prime, const double* aw_prm) { return cuda_complex(" + init + "); }\n";
+    s += R"AWSRC(
+extern "C" __global__ void aw_binit(void* aw_out, int aw_f32, int aw_nrow, int aw_ncol, double aw_dX, double aw_dP,
+                                    const double* aw_prm) {
+  const aw_size_t i = blockIdx.y;
+  const aw_size_t j = (aw_size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= (aw_size_t)aw_ncol) return;
+  const double aw_a = aw_dX * (j - 0.5 * aw_ncol);
+  const double aw_b = aw_dP * (i - 0.5 * aw_nrow);
+  aw_store(aw_out, (long long)i * aw_ncol + j, aw_f32, aw_init_value(i, j, aw_a, aw_b, aw_prm));
+}
+)AWSRC";
+  }
   s += R"AWSRC(
 // 1-D tables of phase factors.  Column entries (aw_ncol of them) sit on the
 // grid x_j = aw_dcol (((j + aw_roll) mod aw_ncol) - aw_ncol/2), row entries on
@@ -141,19 +172,29 @@ inline std::string module_source(const KindNames& kn, const std::string& consts,
 // aw_maskpow > 0 multiplies by the one-dimensional absorbing boundary.
 // With aw_tlist, blockIdx.y = s builds the tables of time aw_tlist[s] + aw_ta at
 // aw_col / aw_row + s * aw_tstride elements (one launch for a run of time points).
+// Batches: blockIdx.z = instance, whose tables sit aw_istride elements apart, with its own
+// parameters (aw_params + instance * aw_np) and, when given, its own aw_ca / aw_shift.
 extern "C" __global__ void aw_tab(void* aw_col, void* aw_row, int aw_f32, int aw_fn, int aw_mode,
                                   int aw_ncol, double aw_dcol, int aw_roll, int aw_nrow, double aw_drow,
                                   double aw_ta, double aw_tb, double aw_ca, double aw_cb, double aw_shift,
-                                  int aw_maskpow, double aw_tmask, const double* aw_tlist, long long aw_tstride) {
+                                  int aw_maskpow, double aw_tmask, const double* aw_tlist, long long aw_tstride,
+                                  const double* aw_params, int aw_np, const double* aw_ca_vec,
+                                  const double* aw_shift_vec, long long aw_istride) {
   const int aw_k = blockIdx.x * blockDim.x + threadIdx.x;
   if (aw_k >= aw_ncol + aw_nrow) return;
+  const int aw_inst = blockIdx.z;
+  const double* aw_prm = aw_params ? aw_params + (long long)aw_inst * aw_np : nullptr;
+  if (aw_ca_vec) aw_ca = aw_ca_vec[aw_inst];
+  if (aw_shift_vec) aw_shift = aw_shift_vec[aw_inst];
+  const int aw_esz = aw_f32 == 1 ? 8 : 16;
+  long long aw_off = aw_inst * aw_istride * aw_esz;
   if (aw_tlist) {
     const int aw_s = blockIdx.y;
     aw_ta += aw_tlist[aw_s];
-    const long long aw_off = aw_s * aw_tstride * (aw_f32 == 1 ? 8 : 16);
-    aw_col = (char*)aw_col + aw_off;
-    aw_row = (char*)aw_row + aw_off;
+    aw_off += aw_s * aw_tstride * aw_esz;
   }
+  aw_col = (char*)aw_col + aw_off;
+  aw_row = (char*)aw_row + aw_off;
   const bool aw_c = aw_k < aw_ncol;
   const int aw_n = aw_c ? aw_ncol : aw_nrow;
   const int aw_idx = aw_c ? aw_k : aw_k - aw_ncol;
@@ -161,15 +202,15 @@ extern "C" __global__ void aw_tab(void* aw_col, void* aw_row, int aw_f32, int aw
   const double aw_x = (aw_c ? aw_dcol : aw_drow) * (aw_m - 0.5 * aw_n);
   double aw_re, aw_im;
   if (aw_mode == 0) {
-    double aw_ph = aw_ca * (aw_fn == 0 ? V(aw_x, aw_ta) : K(aw_x, aw_ta));
-    if (aw_cb != 0.0) aw_ph += aw_cb * (aw_fn == 0 ? V(aw_x, aw_tb) : K(aw_x, aw_tb));
+    double aw_ph = aw_ca * (aw_fn == 0 ? V(aw_x, aw_ta, aw_prm) : K(aw_x, aw_ta, aw_prm));
+    if (aw_cb != 0.0) aw_ph += aw_cb * (aw_fn == 0 ? V(aw_x, aw_tb, aw_prm) : K(aw_x, aw_tb, aw_prm));
     sincos(aw_ph, &aw_im, &aw_re);
   } else {
-    aw_re = exp(aw_ca * ((aw_fn == 0 ? V(aw_x, aw_ta) : K(aw_x, aw_ta)) - aw_shift));
+    aw_re = exp(aw_ca * ((aw_fn == 0 ? V(aw_x, aw_ta, aw_prm) : K(aw_x, aw_ta, aw_prm)) - aw_shift));
     aw_im = 0.0;
   }
   if (aw_maskpow > 0) {
-    double aw_q = aw_mask1(aw_fn, aw_m, aw_x, aw_tmask);
+    double aw_q = aw_mask1(aw_fn, aw_m, aw_x, aw_tmask, aw_prm);
     double aw_f = aw_maskpow == 2 ? aw_q * aw_q : aw_q;
     aw_re *= aw_f;
     aw_im *= aw_f;
@@ -181,11 +222,15 @@ extern "C" __global__ void aw_tab(void* aw_col, void* aw_row, int aw_f32, int aw
 }
 
 // Plain values of V or K on a 1-D grid (Bloch minima, rho_bloch/wigner_bloch fill kernels).
-extern "C" __global__ void aw_values(double* aw_out, int aw_fn, int aw_n, double aw_d, double aw_t) {
+// blockIdx.y = instance of a batch: output row aw_ostride apart, its own parameters
+extern "C" __global__ void aw_values(double* aw_out, int aw_fn, int aw_n, double aw_d, double aw_t,
+                                     const double* aw_params, int aw_np, long long aw_ostride) {
   const int aw_k = blockIdx.x * blockDim.x + threadIdx.x;
   if (aw_k >= aw_n) return;
+  const int aw_inst = blockIdx.y;
+  const double* aw_prm = aw_params ? aw_params + (long long)aw_inst * aw_np : nullptr;
   const double aw_x = aw_d * ((aw_size_t)aw_k - 0.5 * aw_n);
-  aw_out[aw_k] = aw_fn == 0 ? V(aw_x, aw_t) : K(aw_x, aw_t);
+  aw_out[aw_inst * aw_ostride + aw_k] = aw_fn == 0 ? V(aw_x, aw_t, aw_prm) : K(aw_x, aw_t, aw_prm);
 }
 
 // Per-step observables from the marginals of the state.
@@ -205,7 +250,8 @@ extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw
                                        int aw_ncol, int aw_nrow, double aw_dX, double aw_dP, double aw_dXdP,
                                        const int* aw_tslot, const int* aw_tkind, const int* aw_tidx,
                                        const double* aw_tcoef, int aw_nterms, int aw_nslots,
-                                       int aw_cstride, int aw_proll, int aw_pnorm_own, int aw_sqrt_norm) {
+                                       int aw_cstride, int aw_proll, int aw_pnorm_own, int aw_sqrt_norm,
+                                       const double* aw_prm) {
   __shared__ double aw_red[256];
   __shared__ double aw_tv[64];
   if (aw_stop && *aw_stop) return;
@@ -233,12 +279,12 @@ extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw
     if (aw_tkind[aw_k] == 0) {
       for (int aw_j = aw_t; aw_j < aw_ncol; aw_j += aw_nt) {
         const double X = aw_dX * ((aw_size_t)aw_j - 0.5 * aw_ncol);
-        aw_s += aw_colsum[(long long)aw_j * aw_cstride] * aw_obs_x(aw_idx, X, t);
+        aw_s += aw_colsum[(long long)aw_j * aw_cstride] * aw_obs_x(aw_idx, X, t, aw_prm);
       }
     } else {
       for (int aw_i = aw_t; aw_i < aw_nrow; aw_i += aw_nt) {
         const double P = aw_dP * ((aw_size_t)((aw_i + aw_proll) % aw_nrow) - 0.5 * aw_nrow);
-        aw_s += aw_rowsum[aw_i] * aw_obs_p(aw_idx, P, t);
+        aw_s += aw_rowsum[aw_i] * aw_obs_p(aw_idx, P, t, aw_prm);
       }
     }
     const double aw_v = aw_block_sum(aw_s, aw_red);
@@ -279,10 +325,23 @@ extern "C" __global__ void aw_finalize_rot(const double2* aw_z, const double2* a
                                            double t, int aw_ncol, int aw_nrow, double aw_dX, double aw_dP,
                                            double aw_dXdP, const int* aw_tslot, const int* aw_tkind,
                                            const int* aw_tidx, const double* aw_tcoef, int aw_nterms, int aw_nslots,
-                                           int aw_nchunk) {
-  // blocks: (term or norm or purity) x chunk; FP64 expression evaluation spread over the GPU
+                                           int aw_nchunk, const double* aw_params, int aw_np, long long aw_hstride) {
+  // blocks: (term or norm or purity) x chunk; FP64 expression evaluation spread over the GPU.
+  // blockIdx.y = instance of a batch, with its own marginals, partials, history row and scalars.
   __shared__ double aw_red[256];
   __shared__ int aw_is_last;
+  {
+    const long long aw_in = blockIdx.y;
+    aw_z += aw_in * aw_ncol;
+    aw_wpart += aw_in * aw_nparts * aw_nrow;
+    if (aw_abs2) aw_abs2 += aw_in * aw_nb2;
+    aw_tv += aw_in * gridDim.x;
+    aw_counter += aw_in;
+    aw_hist += aw_in * aw_hstride;
+    aw_inv_norm += 2 * aw_in;
+    if (aw_stop) aw_stop += aw_in;
+  }
+  const double* aw_prm = aw_params ? aw_params + (long long)blockIdx.y * aw_np : nullptr;
   if (aw_stop && *aw_stop) return;
   const int aw_q = blockIdx.x / aw_nchunk;      // 0..nterms-1 terms, nterms norm, nterms+1 purity
   const int aw_c = blockIdx.x - aw_q * aw_nchunk;
@@ -296,7 +355,7 @@ extern "C" __global__ void aw_finalize_rot(const double2* aw_z, const double2* a
       for (int aw_j = aw_lo + aw_t; aw_j < aw_lo + aw_len; aw_j += aw_nt) {
         const double X = aw_dX * ((aw_size_t)aw_j - 0.5 * aw_ncol);
         const double aw_cj = ((aw_j & 1) ? -1.0 : 1.0) * aw_nrow * aw_z[aw_j].x;
-        aw_s += aw_cj * aw_obs_x(aw_idx, X, t);
+        aw_s += aw_cj * aw_obs_x(aw_idx, X, t, aw_prm);
       }
     } else {
       const int aw_len = aw_nrow / aw_nchunk, aw_lo = aw_c * aw_len;
@@ -305,7 +364,7 @@ extern "C" __global__ void aw_finalize_rot(const double2* aw_z, const double2* a
         const int aw_k = (aw_nrow - aw_i) & (aw_nrow - 1);
         double aw_w = 0.0;
         for (int aw_p = 0; aw_p < aw_nparts; ++aw_p) aw_w += aw_wpart[(long long)aw_p * aw_nrow + aw_k].x;
-        aw_s += ((aw_i & 1) ? -1.0 : 1.0) * aw_nrow * aw_w * aw_obs_p(aw_idx, P, t);
+        aw_s += ((aw_i & 1) ? -1.0 : 1.0) * aw_nrow * aw_w * aw_obs_p(aw_idx, P, t, aw_prm);
       }
     }
   } else if (aw_q == aw_nterms) {
@@ -348,17 +407,21 @@ extern "C" __global__ void aw_finalize_rot(const double2* aw_z, const double2* a
 
 // 2-D absorbing boundaries of the rotated frame (expV / expK of
 // wigner_moyal_cuda_1d.py:742-778 multiply by these expressions).
+// blockIdx.z = instance of a batch: mask aw_nrow * aw_ncol elements apart, its own parameters
 extern "C" __global__ void aw_mask2d(void* aw_out, int aw_f32, int aw_which, double t, int aw_nrow, int aw_ncol,
-                                     double aw_dXX, double aw_dXXp, double aw_dPP, double aw_dPPp) {
+                                     double aw_dXX, double aw_dXXp, double aw_dPP, double aw_dPPp,
+                                     const double* aw_params, int aw_np) {
   const aw_size_t i = blockIdx.y;
+  const double* aw_prm = aw_params ? aw_params + (long long)blockIdx.z * aw_np : nullptr;
+  aw_out = (char*)aw_out + (long long)blockIdx.z * aw_nrow * aw_ncol * (aw_f32 == 1 ? 4 : 8);
   const aw_size_t j = (aw_size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= (aw_size_t)aw_ncol) return;
   const double XX = aw_dXX * (j - 0.5 * aw_ncol);
   const double XX_prime = aw_dXXp * (i - 0.5 * aw_nrow);
   const double PP = aw_dPP * (j - 0.5 * aw_ncol);
   const double PP_prime = aw_dPPp * (i - 0.5 * aw_nrow);
-  const double aw_v = aw_which == 0 ? aw_absx2d(i, j, XX, XX_prime, PP, PP_prime, t)
-                                    : aw_absp2d(i, j, XX, XX_prime, PP, PP_prime, t);
+  const double aw_v = aw_which == 0 ? aw_absx2d(i, j, XX, XX_prime, PP, PP_prime, t, aw_prm)
+                                    : aw_absp2d(i, j, XX, XX_prime, PP, PP_prime, t, aw_prm);
   const long long aw_k = (long long)i * aw_ncol + j;
   if (aw_f32 == 1) ((float*)aw_out)[aw_k] = (float)aw_v;
   else if (aw_f32 == 2) ((float2*)aw_out)[aw_k] = aw_df1(aw_v);

@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(NT) aw_pass_kernel(const __grid_constant__ AwP
   constexpr int E = Own<Tile, NT>::E;
   constexpr int STEP = Own<Tile, NT>::STEP;
   __shared__ double red[NT];
-  const int inst = blockIdx.y;
+  const int inst = blockIdx.y + a.inst0;
   if (a.stop && a.stop[inst]) return;
   const int tid = threadIdx.x;
   const int line = tid % L;

@@ -66,6 +66,7 @@ typedef struct AwPassArgs {
   const int* stop;          // when non-zero the pass is skipped
   long long batch_elems;    // batched launches: elements per instance (blockIdx.y)
   long long batch_tab;      // ... table entries per instance
+  int inst0;                // instance of blockIdx.y = 0 (a launch over a range of a batch's instances)
 } AwPassArgs;
 
 // Host-side launchers, one per precision (aw_pass_f64.cu / aw_pass_f32.cu).

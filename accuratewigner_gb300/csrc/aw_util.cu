@@ -37,16 +37,18 @@ __device__ __forceinline__ void st(void* p, long long k, int f32, double2 v) {
   }
 }
 
+// a *= (re + i im) * ptr[2 inst .. 2 inst + 1]; instance inst = blockIdx.y holds n elements
 __global__ void k_scale(void* a, int f32, long long n, double re, double im, const double* ptr) {
+  const long long inst = blockIdx.y;
   double sr = re, si = im;
   if (ptr) {
-    const double pr = ptr[0], pi = ptr[1];
+    const double pr = ptr[2 * inst], pi = ptr[2 * inst + 1];
     sr = re * pr - im * pi;
     si = re * pi + im * pr;
   }
   for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
-    double2 v = ld(a, k, f32);
-    st(a, k, f32, make_double2(v.x * sr - v.y * si, v.x * si + v.y * sr));
+    double2 v = ld(a, inst * n + k, f32);
+    st(a, inst * n + k, f32, make_double2(v.x * sr - v.y * si, v.x * si + v.y * sr));
   }
 }
 
@@ -114,9 +116,19 @@ __global__ void k_psi2rho(const void* psi, int f32, int N, void* rho) {
 // 1 / (Tr rho * dX) with the complex trace (rho_bloch_cuda_1d.py:244).  The
 // purity Sum |rho|^2 dX^2 (rho_vneumann_cuda_1d.py:565-579) of the normalised
 // state follows from the row pass's |rho|^2 partials.
+// blockIdx.x = instance: diag n apart, abs2part nparts apart, inv_out 2 apart, hist hstride apart
 __global__ void k_trace_finalize(const double2* diag, int n, const double* abs2part, int nparts, double dX,
-                                 int complex_trace, double* inv_out, double* hist, int* stop, int stop_on_purity) {
+                                 int complex_trace, double* inv_out, double* hist, long long hstride, int* stop,
+                                 int stop_on_purity) {
   __shared__ double rr[256], ri[256], ra[256];
+  {
+    const long long in = blockIdx.x;
+    diag += in * n;
+    if (abs2part) abs2part += in * nparts;
+    inv_out += 2 * in;
+    if (hist) hist += in * hstride;
+    if (stop) stop += in;
+  }
   if (stop && *stop) return;
   const int t = threadIdx.x;
   double sr = 0.0, si = 0.0, sa = 0.0;
@@ -248,7 +260,11 @@ inline int ok() { return cudaGetLastError() == cudaSuccess ? 0 : -1; }
 extern "C" {
 
 int aw_k_scale(void* a, int f32, long long n, double re, double im, const double* ptr, void* s) {
-  k_scale<<<grid_for(n), 256, 0, (cudaStream_t)s>>>(a, f32, n, re, im, ptr);
+  return aw_k_scale_n(a, f32, n, 1, re, im, ptr, s);
+}
+int aw_k_scale_n(void* a, int f32, long long n, int ninst, double re, double im, const double* ptr, void* s) {
+  const int gx = (grid_for(n) + ninst - 1) / ninst;
+  k_scale<<<dim3(gx, ninst), 256, 0, (cudaStream_t)s>>>(a, f32, n, re, im, ptr);
   return ok();
 }
 int aw_k_fill(void* a, int f32, long long n, double re, double im, void* s) {
@@ -273,8 +289,14 @@ int aw_k_psi2rho(const void* psi, int f32, int N, void* rho, void* s) {
 }
 int aw_k_trace_finalize(const double2* diag, int n, const double* abs2part, int nparts, double dX, int complex_trace,
                         double* inv_out, double* hist, int* stop, int stop_on_purity, void* s) {
-  k_trace_finalize<<<1, 256, 0, (cudaStream_t)s>>>(diag, n, abs2part, nparts, dX, complex_trace, inv_out, hist, stop,
-                                                   stop_on_purity);
+  return aw_k_trace_finalize_n(diag, n, abs2part, nparts, dX, complex_trace, inv_out, hist, 0, stop, stop_on_purity, 1,
+                               s);
+}
+int aw_k_trace_finalize_n(const double2* diag, int n, const double* abs2part, int nparts, double dX, int complex_trace,
+                          double* inv_out, double* hist, long long hstride, int* stop, int stop_on_purity, int ninst,
+                          void* s) {
+  k_trace_finalize<<<ninst, 256, 0, (cudaStream_t)s>>>(diag, n, abs2part, nparts, dX, complex_trace, inv_out, hist,
+                                                       hstride, stop, stop_on_purity);
   return ok();
 }
 int aw_k_norm_finalize(const double* parts, int nparts, double scale, double* inv_out, double* hist, void* s) {

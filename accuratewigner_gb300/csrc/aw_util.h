@@ -7,6 +7,8 @@ extern "C" {
 #endif
 
 int aw_k_scale(void* a, int f32, long long n, double re, double im, const double* ptr, void* s);
+// ninst instances of n elements, instance k scaled by ptr[2k..2k+1] (when ptr)
+int aw_k_scale_n(void* a, int f32, long long n, int ninst, double re, double im, const double* ptr, void* s);
 int aw_k_fill(void* a, int f32, long long n, double re, double im, void* s);
 int aw_k_convert(const void* src, int sf32, void* dst, int df32, long long n, void* s);
 int aw_k_partial(const void* a, int f32, long long n, int mode, long long stride, double2* part, int nblocks, void* s);
@@ -14,6 +16,9 @@ int aw_k_embed(const void* rho, int f32, int N, void* W, int M, int pad, void* s
 int aw_k_psi2rho(const void* psi, int f32, int N, void* rho, void* s);
 int aw_k_trace_finalize(const double2* diag, int n, const double* abs2part, int nparts, double dX, int complex_trace,
                         double* inv_out, double* hist, int* stop, int stop_on_purity, void* s);
+int aw_k_trace_finalize_n(const double2* diag, int n, const double* abs2part, int nparts, double dX, int complex_trace,
+                          double* inv_out, double* hist, long long hstride, int* stop, int stop_on_purity, int ninst,
+                          void* s);
 int aw_k_set2(double* p, double a, double b, void* s);
 int aw_k_sum_parts(const double2* part, int nparts, int n, double2* out, void* s);
 int aw_k_norm_finalize(const double* parts, int nparts, double scale, double* inv_out, double* hist, void* s);

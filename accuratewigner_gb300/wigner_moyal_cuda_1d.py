@@ -9,7 +9,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._common import (ExprInfo, Handle, TermTable, assert_pow2, bind_kwargs, cuda_defines, define_value, mask_mode,
+from ._common import (apply_batch, ExprInfo, Handle, TermTable, assert_pow2, bind_kwargs, cuda_defines, define_value, mask_mode,
                       precision_code, require)
 
 _c = ctypes
@@ -150,6 +150,7 @@ class WignerMoyalCUDA1D:
         else:
             TermTable(info).fill(cfg, keep)
         self._n_slots = cfg.n_slots
+        apply_batch(cfg, kwargs, keep)
         self._handle = Handle(cfg)
         self._h = self._handle._h
 

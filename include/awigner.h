@@ -94,7 +94,37 @@ typedef struct aw_config {
   const double* term_coef;
   int32_t n_slots;
   int32_t obs_p_time_dependent; /* a P-only observable mentions t */
+  /* Batches (no reference counterpart: the batched and served forms).  n_inst > 1 makes the
+   * handle hold n_inst independent instances of the same kind and grid, stepped together by
+   * every call; each has its own state, tables, norm, stop flag and observable history.
+   * param_names are per-instance constants usable in V, K, the absorbing boundaries, the
+   * observables and init_expr; values are set per instance with aw_set_params.  init_expr is
+   * the initial state of an instance (W(X, P) for Wigner-Moyal / Wigner-Bloch, rho(X, X_prime)
+   * for von Neumann / rho-Bloch), evaluated by aw_init_state.  Batches require V and K that do
+   * not depend on t.  n_inst = 0 or 1 with n_params = 0 is the plain single propagator. */
+  int32_t n_inst;
+  int32_t n_params;
+  const char* const* param_names;
+  const char* init_expr;
 } aw_config;
+
+/* Batches: the view [first, first + count) of instances that the following calls act on
+ * (state buffers, fills, sums, transforms, propagation); the full range after aw_create.
+ * aw_set_params writes instance `inst`'s parameter row (n_params values); aw_set_active marks
+ * which instances of the view the step loops advance (inactive ones keep their state);
+ * aw_init_state evaluates init_expr for the view and normalises it as set_wignerfunction /
+ * set_rho do (wigner_moyal_cuda_1d.py:379-420, rho_vneumann_cuda_1d.py:348-385);
+ * aw_history_of reads one instance's observable rows of the last propagation;
+ * aw_gibbs_batch runs `steps` Bloch steps on the view with a step dbeta[k] per instance and
+ * reports per-instance steps done and purity (wigner_bloch_cuda_1d.py:119-155,
+ * rho_bloch_cuda_1d.py:125-161). */
+int aw_set_view(aw_handle h, int32_t first, int32_t count);
+int aw_set_params(aw_handle h, int32_t inst, const double* values);
+int aw_set_active(aw_handle h, const int32_t* flags);
+int aw_init_state(aw_handle h);
+int aw_history_of(aw_handle h, int32_t inst, double* out, int64_t max_rows, int64_t* rows, int32_t* cols);
+int aw_gibbs_batch(aw_handle h, const double* dbeta, int64_t steps, int64_t* done, double* purity);
+int aw_bloch_min_of(aw_handle h, int32_t inst, double* v_min, double* k_min);
 
 /* library */
 int32_t aw_version(void);
