@@ -107,7 +107,8 @@ class PropagatorBatch:
         Instance k runs round(1 / (kT[k] dbeta)) steps of its re-fitted dbeta and stops early once
         its purity reaches 1.  The instances must be ordered by step count (non-decreasing), so
         that the instances still running always form the tail of the batch.
-        Returns (steps done, last purity) per instance.
+        Returns (steps done, last purity) per instance; self.energy holds the last <H> of each
+        Wigner-Bloch instance.
         """
         dbeta = self.prop.dbeta if dbeta is None else dbeta
         kT = np.broadcast_to(np.asarray(kT, dtype=np.float64), (self.n_inst,))
@@ -120,6 +121,9 @@ class PropagatorBatch:
         self.init_state()
         done = np.zeros(self.n_inst, np.int64)
         purity = np.zeros(self.n_inst)
+        # Wigner-Bloch records <H> every step (first Bloch observable slot)
+        h_slot = self.prop._bloch_slots[0] if hasattr(self.prop, "_bloch_slots") else None
+        self.energy = np.full(self.n_inst, np.nan)
         running = np.ones(self.n_inst, bool)
         ran_before = 0
         first = 0
@@ -134,6 +138,8 @@ class PropagatorBatch:
                     done[k] += d[k - first]
                     if d[k - first] > 0:
                         purity[k] = p[k - first]
+                        if h_slot is not None:
+                            self.energy[k] = self.history(k)[d[k - first] - 1, h_slot]
                     if d[k - first] < chunk:
                         running[k] = False  # stopped at purity >= 1
                 ran_before = int(nsteps[first])

@@ -1825,6 +1825,7 @@ static int rot_gibbs(aw_state_s* h, const double* dbeta, long long steps, long l
     if (done) done[k] = ran[k];
     if (purity && ran[k] > 0) purity[k] = hk[(size_t)(ran[k] - 1) * cols + cols - 2];
   }
+  h->hist_rows = steps;  // rows 0 .. done - 1 of each instance hold its per-step observables
   // rho_n of the last executed step (position representation, unnormalised) and its W, for the
   // instances that ran
   TRY(settle(h));

@@ -23,8 +23,9 @@ template <typename V, int N, int LINES> struct Shape {
   static constexpr int TILE = N * LINES;
   static constexpr int E = TILE / 1024 > 8 ? TILE / 1024 : 8;
   static constexpr int NT = TILE / E;
-  static constexpr int SMEM_ELEMS = LINES > 1 ? (N + 1) * LINES : N;  // upper bound over both tile kinds
-  static constexpr bool FITS = (N + 1) * LINES * (int)sizeof(V) <= 128 * 1024;
+  // the tile fits the 128 KB a block is given: rows are padded by one element when LINES > 1
+  static constexpr bool FITS_ROW = (LINES > 1 ? (N + 1) * LINES : N) * (int)sizeof(V) <= 128 * 1024;
+  static constexpr bool FITS_COL = N * LINES * (int)sizeof(V) <= 128 * 1024;
 };
 
 template <typename V> struct RealOf;
@@ -320,19 +321,19 @@ inline int choose_row_lines(int ncols, int esz) {
   return l;
 }
 
-// columns per column-pass block: as many as fit (<= 16, <= 128 KB of shared memory) while the
-// launch still has at least 4 blocks per SM
+// columns per column-pass block: as many as fit (<= 16, <= 128 KB of shared memory, <= 512
+// threads so that the 16-byte element types keep their registers)
 inline int max_col_lines(int nrows, int ncols, int esz) {
   int b = 16;
-  while (b > 1 && ((long long)nrows * b * esz > 128 * 1024 || ncols % b)) b >>= 1;
+  while (b > 1 && ((long long)nrows * b * esz > 128 * 1024 || (long long)nrows * b > 4096 || ncols % b))
+    b >>= 1;
   return b;
 }
 
 inline int choose_col_lines(int nrows, int ncols, int batch, int esz) {
   // as many columns as fit while the launch keeps at least 4 blocks per SM
-  int b = 16;
-  while (b > 1 && ((long long)nrows * b * esz > 128 * 1024 || (long long)(ncols / b) * batch < 4 * AW_SMS || ncols % b))
-    b >>= 1;
+  int b = max_col_lines(nrows, ncols, esz);
+  while (b > 1 && (long long)(ncols / b) * batch < 4 * AW_SMS) b >>= 1;
   return b;
 }
 
@@ -351,7 +352,7 @@ static int prepare_smem(K kern, size_t max_dynamic) {
 template <typename V, int N, int LINES>
 static int launch_row_t(const AwPassArgs* a, int batch, cudaStream_t st) {
   typedef Shape<V, N, LINES> S;
-  if constexpr (!S::FITS) {
+  if constexpr (!S::FITS_ROW) {
     return -5;
   } else {
     typedef RowTile<N, LINES> Tile;
@@ -369,7 +370,7 @@ static int launch_row_t(const AwPassArgs* a, int batch, cudaStream_t st) {
 template <typename V, int N, int LINES>
 static int launch_col_t(const AwPassArgs* a, int batch, cudaStream_t st) {
   typedef Shape<V, N, LINES> S;
-  if constexpr (!S::FITS) {
+  if constexpr (!S::FITS_COL) {
     return -5;
   } else {
     typedef ColTile<N, LINES> Tile;

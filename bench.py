@@ -12,6 +12,14 @@ A "step" is one split step including its per-step Wigner transform,
 normalisation and observables.  The metric is grid-point * steps / s.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision c128|c128-fp64|c64]
+
+Other workloads (one JSON line each, not the headline):
+  --workload plain          Wigner-Moyal 256 x 256, anharmonic, Ehrenfest every step, 1000 steps
+  --workload batched-gibbs  64 Wigner-Bloch Gibbs states of 512 x 512 in one batch, per-instance
+                            double well and temperature; purity and energy against complex128
+  --workload served         Poisson stream of Wigner-Moyal / von Neumann / rho-Bloch requests through
+                            the continuous-batching loop: p50 / p99 latency and aggregate throughput
+  --workload large-vn       von Neumann 4096 x 4096, driven Morse potential, 2000 steps
 """
 import argparse
 import ctypes
@@ -367,6 +375,157 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+# ------------------------------------------------------------------------ other workloads
+def _timed(fn):
+    import torch
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, out
+
+
+def _line(workload, metric, value, unit, seconds, args, config, extra=None, higher=True):
+    line = {"workload": workload, "metric": metric, "value": value, "unit": unit, "n_gpus": 1,
+            "seconds": seconds, "higher_is_better": higher, "dtype": DTYPE[args.precision],
+            "data": "synthetic, seeded", "config": config}
+    line.update(extra or {})
+    print(json.dumps(line))
+
+
+def run_plain(args):
+    """Wigner-Moyal 256 x 256, Xa = 8, Pa = 7, V = x^2 / 2 + 0.05 x^4, dt = 0.01, 1000 steps with Ehrenfest."""
+    from accuratewigner_gb300 import WignerMoyalCUDA1D
+
+    p = dict(t=0.0, dt=0.01, X_gridDIM=256, X_amplitude=8.0, P_gridDIM=256, P_amplitude=7.0, K="0.5 * P * P",
+             V="0.5 * X * X + 0.05 * X * X * X * X", diff_K="P", diff_V="X + 0.2 * X * X * X",
+             precision=args.precision)
+    g = WignerMoyalCUDA1D(**p)
+    g.set_wignerfunction("exp(-pow(X - 1., 2) - P * P) / M_PI")
+    g.propagate(20)
+    steps = 1000
+    with ClockSampler(0) as clk:
+        sec, _ = _timed(lambda: [g.propagate(CHUNK) for _ in range(steps // CHUNK)])
+    _line("plain", "grid-pt*steps/s", 256 * 256 * steps / sec, "grid-pt*steps/s", sec, args,
+          {"grid": [256, 256], "steps": steps, "steps_per_call": CHUNK, "precision": args.precision},
+          {"ms_per_step": sec / steps * 1e3, "clocks": clk.summary()})
+
+
+def run_batched_gibbs(args):
+    """64 Wigner-Bloch instances of 512 x 512 (Xa = 10, Pa = 8), V = a x^4 - b x^2 with a ~ U(0.02, 0.1),
+    b ~ U(0.2, 1.0), beta ~ LogU(0.5, 20), dbeta = 0.01, all in one batch."""
+    from accuratewigner_gb300 import WignerBlochCUDA1D
+    from accuratewigner_gb300.batch import PropagatorBatch, dbeta_num_beta_steps
+
+    n_inst, n = 64, 512
+    rng = np.random.default_rng(0)
+    a = rng.uniform(0.02, 0.1, n_inst)
+    b = rng.uniform(0.2, 1.0, n_inst)
+    beta = np.exp(rng.uniform(np.log(0.5), np.log(20.0), n_inst))
+    kT = 1.0 / beta
+    steps = np.array([dbeta_num_beta_steps(k, 0.01)[1] for k in kT])
+    order = np.argsort(steps, kind="stable")  # instances ordered by step count
+    base = dict(t=0.0, X_gridDIM=n, P_gridDIM=n, X_amplitude=10.0, P_amplitude=8.0, K="0.5 * P * P",
+                V="a * X * X * X * X - b * X * X", dt=0.01, dbeta=0.01, kT=1.0, t_initial=0.0)
+
+    def run(prec):
+        bt = PropagatorBatch(WignerBlochCUDA1D, n_inst, params=("a", "b"), init="1.", precision=prec, **base)
+        for slot, k in enumerate(order):
+            bt.set_params(slot, [a[k], b[k]])
+        bt.gibbs(kT[order])  # warm-up (JIT, buffers)
+        sec, (done, pur) = _timed(lambda: bt.gibbs(kT[order]))
+        e = bt.energy.copy()
+        bt.close()
+        return sec, done, pur, e
+
+    with ClockSampler(0) as clk:
+        sec, done, pur, e = run(args.precision)
+    ref = run("c128") if args.precision != "c128" else None
+    work = float(np.sum(done)) * n * n
+    extra = {"ms_total": sec * 1e3, "instances": n_inst, "steps_total": int(np.sum(done)),
+             "purity_range": [float(pur.min()), float(pur.max())], "clocks": clk.summary()}
+    if ref:
+        extra["vs_c128"] = {"max_abs_purity_err": float(np.max(np.abs(pur - ref[2]))),
+                            "max_rel_energy_err": float(np.max(np.abs(e - ref[3]) / np.abs(ref[3])))}
+    _line("batched-gibbs", "grid-pt*steps/s", work / sec, "grid-pt*steps/s", sec, args,
+          {"instances": n_inst, "grid": [n, n], "X_amplitude": 10.0, "P_amplitude": 8.0, "dbeta": 0.01,
+           "beta": "LogU(0.5, 20), seed 0", "potential": "a x^4 - b x^2, a ~ U(0.02, 0.1), b ~ U(0.2, 1.0)",
+           "precision": args.precision}, extra)
+
+
+def run_served(args):
+    """Poisson stream of Wigner-Moyal / von Neumann / rho-Bloch requests, sides {128 .. 2048},
+    steps ~ U(100, 5000), through the continuous-batching request loop."""
+    from accuratewigner_gb300.serve import Engine, make_stream
+
+    eng = Engine(precision=args.precision, chunk=200)
+    eng.warm()
+    reqs = make_stream(args.requests, args.rate, seed=0)
+    with ClockSampler(0) as clk:
+        wall = eng.run(reqs)
+    eng.close()
+    lat = np.array([r.latency for r in reqs])
+    work = float(sum(r.work for r in reqs))
+    by_kind = {k: float(np.percentile([r.latency for r in reqs if r.kind == k], 50))
+               for k in ("wm", "vn", "rb") if any(r.kind == k for r in reqs)}
+    _line("served", "grid-pt*steps/s (aggregate) with p50/p99 request latency", work / wall, "grid-pt*steps/s",
+          wall, args,
+          {"requests": args.requests, "rate_per_s": args.rate, "seed": 0, "sides": [128, 256, 512, 1024, 2048],
+           "steps": "U(100, 5000)", "kinds": ["wigner-moyal (Ehrenfest)", "von Neumann", "rho-Bloch Gibbs"],
+           "potential": "c2 x^2 + c3 x^3 + c4 x^4, c2 ~ U(0.1, 1), c3 ~ U(-0.02, 0.02), c4 ~ U(0, 0.05)",
+           "amplitude": "X_amplitude = P_amplitude = sqrt(pi N / 2)", "chunk_steps": 200,
+           "precision": args.precision},
+          {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+           "mean_latency_s": float(lat.mean()), "p50_latency_by_kind_s": by_kind, "clocks": clk.summary()})
+
+
+def run_large_vn(args):
+    """von Neumann 4096 x 4096, X_amplitude = 80, Morse V = D (1 - exp(-alpha (x - x0)))^2 + x 0.02 sin(0.01 t)
+    (D = 0.18, alpha = 1, x0 = 1.4), dt = 0.02, 2000 steps; rho0 = sum of 8 seeded Gaussian pure states."""
+    from accuratewigner_gb300 import RhoVNeumannCUDA1D
+
+    n, steps = 4096, args.steps if args.steps != 200 else 2000
+    p = dict(t=0.0, dt=0.02, X_gridDIM=n, X_amplitude=80.0, D=0.18, alpha=1.0, xm=1.4, K="0.5 * P * P",
+             V="D * pow(1. - exp(-alpha * (X - xm)), 2) + X * 0.02 * sin(0.01 * t)", diff_K="P",
+             diff_V="2. * D * alpha * exp(-alpha * (X - xm)) * (1. - exp(-alpha * (X - xm))) + 0.02 * sin(0.01 * t)")
+    rng = np.random.default_rng(0)
+    centres = rng.uniform(-3.0, 6.0, 8)
+    w = rng.uniform(0.2, 1.0, 8)
+    w /= w.sum()
+    x = np.linspace(-80.0, 80.0 - 160.0 / n, n)
+
+    def rho0():
+        r = np.zeros((n, n))
+        for c, wk in zip(centres, w):
+            g = np.exp(-0.5 * (x - c) ** 2)
+            r += wk * np.outer(g, g)
+        return r
+
+    def run(prec, k):
+        g = RhoVNeumannCUDA1D(precision=prec, **p)
+        g.set_rho(rho0())
+        g.propagate(3)
+        sec, _ = _timed(lambda: [g.propagate(min(CHUNK, k - i)) for i in range(0, k, CHUNK)])
+        out = (sec, g.rho.get(), np.array(g.X_average), g.get_purity())
+        g._handle.close()
+        return out
+
+    with ClockSampler(0) as clk:
+        sec, rho, xav, pur = run(args.precision, steps)
+    bytes_per_pt = 4 * STATE_BYTES_PER_PT[args.precision]
+    extra = {"ms_per_step": sec / steps * 1e3, "achieved_gbs": bytes_per_pt * n * n * steps / sec / 1e9,
+             "algorithmic_bytes_per_pt_step": bytes_per_pt, "trace": float(np.trace(rho).real * 160.0 / n),
+             "purity": float(pur), "x_final": float(xav[-1]), "clocks": clk.summary()}
+    if args.precision != "c128":
+        _, rref, xref, pref = run("c128", steps)
+        extra["vs_c128"] = {"rho_rel_l2": float(np.linalg.norm(rho - rref) / np.linalg.norm(rref)),
+                            "x_max_abs_err": float(np.max(np.abs(xav - xref))), "purity_err": float(abs(pur - pref))}
+    _line("large-vn", "grid-pt*steps/s", n * n * steps / sec, "grid-pt*steps/s", sec, args,
+          {"grid": [n, n], "X_amplitude": 80.0, "dt": 0.02, "steps": steps, "initial": "8 Gaussians, seed 0",
+           "precision": args.precision}, extra)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -375,9 +534,20 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="c128", choices=["c128", "c128-fp64", "c64"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="strong-field",
+                    choices=["strong-field", "plain", "batched-gibbs", "served", "large-vn"])
+    ap.add_argument("--requests", type=int, default=60, help="served: number of requests")
+    ap.add_argument("--rate", type=float, default=1.2, help="served: Poisson arrival rate per second")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    other = {"plain": run_plain, "batched-gibbs": run_batched_gibbs, "served": run_served, "large-vn": run_large_vn}
+    if args.workload in other:
+        import torch
+
+        torch.cuda.init()
+        other[args.workload](args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
