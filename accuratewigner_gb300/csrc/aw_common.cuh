@@ -56,6 +56,25 @@ template <> __device__ __forceinline__ dfr to_acc<dfr>(float v) { return df_from
 template <typename A> __device__ __forceinline__ A to_acc(dfr v);
 template <> __device__ __forceinline__ dfr to_acc<dfr>(dfr v) { return v; }
 
+// partial sums exchanged between the blocks of a cluster: FP64 for the native types, the working
+// double-float form for dfc (converted to FP64 once, after the cluster sum)
+template <typename V> struct cpart {
+  typedef double2 type;
+  __device__ static double2 make(typename scalar_of<V>::type x, typename scalar_of<V>::type y) {
+    return make_double2(to_d(x), to_d(y));
+  }
+  __device__ static double2 zero() { return make_double2(0.0, 0.0); }
+  __device__ static double2 add(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+  __device__ static double2 to_d2(double2 a) { return a; }
+};
+template <> struct cpart<dfc> {
+  typedef dfc type;
+  __device__ static dfc make(dfr x, dfr y) { return dfc{x, y}; }
+  __device__ static dfc zero() { return dfc{dfr{0.f, 0.f}, dfr{0.f, 0.f}}; }
+  __device__ static dfc add(dfc a, dfc b) { return dfc_add(a, b); }
+  __device__ static double2 to_d2(dfc a) { return dfc_to_double2(a); }
+};
+
 template <typename V>
 __device__ __forceinline__ V cmake(typename scalar_of<V>::type x, typename scalar_of<V>::type y) {
   V r;

@@ -15,17 +15,18 @@
 namespace cg = cooperative_groups;
 
 // Tile shapes.  A row tile holds LINES whole rows, a column tile a slab of
-// LINES whole columns; a thread keeps E elements (8, more for lines longer
-// than 8192 elements so that a block stays at or below 1024 threads).  The
-// number of lines per tile is chosen at run time (aw_row_pass_lines /
-// aw_col_pass_lines) so that a launch spreads over all 152 SMs.
+// LINES whole columns; a thread keeps E elements (8, more for tiles above
+// 4096 elements so that a block stays at or below 512 threads and 128
+// registers a thread).  The number of lines per tile is chosen at run time
+// (aw_row_pass_lines / aw_col_pass_lines) so that a launch spreads over all
+// 152 SMs; column tiles hold at most 4096 elements.
 template <typename V, int N, int LINES> struct Shape {
   static constexpr int TILE = N * LINES;
-  static constexpr int E = TILE / 1024 > 8 ? TILE / 1024 : 8;
+  static constexpr int E = TILE / 512 > 8 ? TILE / 512 : 8;
   static constexpr int NT = TILE / E;
   // the tile fits the 128 KB a block is given: rows are padded by one element when LINES > 1
   static constexpr bool FITS_ROW = (LINES > 1 ? (N + 1) * LINES : N) * (int)sizeof(V) <= 128 * 1024;
-  static constexpr bool FITS_COL = N * LINES * (int)sizeof(V) <= 128 * 1024;
+  static constexpr bool FITS_COL = N * LINES * (int)sizeof(V) <= 128 * 1024 && (N * LINES <= 4096 || LINES == 1);
 };
 
 template <typename V> struct RealOf;
@@ -133,7 +134,9 @@ __device__ __forceinline__ double block_sum(double x, double* red, int tid) {
 }
 
 template <typename V, class Tile, int NT>
-__global__ void __launch_bounds__(NT) aw_pass_kernel(const __grid_constant__ AwPassArgs a) {
+// At most 128 registers a thread (4 blocks of 128 threads, 2 of 256 per SM): the double-float
+// passes are latency-bound, and the occupancy gained beats the few registers they would use beyond.
+__global__ void __launch_bounds__(NT, (NT <= 128 ? 4 : (NT <= 256 ? 2 : 1))) aw_pass_kernel(const __grid_constant__ AwPassArgs a) {
   extern __shared__ __align__(16) unsigned char aw_smem[];
   typedef typename RealOf<V>::type T;
   V* s = reinterpret_cast<V*>(aw_smem);
@@ -237,7 +240,8 @@ __global__ void __launch_bounds__(NT) aw_pass_kernel(const __grid_constant__ AwP
           }
           if (line == 0) {
             if (a.cluster > 1)
-              reinterpret_cast<double2*>(aw_smem + sizeof(V) * Tile::SMEM_ELEMS)[pos] = make_double2(to_d(xr), to_d(xi));
+              reinterpret_cast<typename cpart<V>::type*>(aw_smem + sizeof(V) * Tile::SMEM_ELEMS)[pos] =
+                  cpart<V>::make(xr, xi);
             else
               a.alt_cross[((long long)inst * gridDim.x + blockIdx.x) * a.nrows + pos] = make_double2(to_d(xr), to_d(xi));
           }
@@ -264,15 +268,12 @@ __global__ void __launch_bounds__(NT) aw_pass_kernel(const __grid_constant__ AwP
         const int ncl = (int)cl.num_blocks();
         const int n = a.nrows;
         const int lo = rank * (n / ncl), hi = lo + n / ncl;
-        double2* mine = reinterpret_cast<double2*>(aw_smem + sizeof(V) * Tile::SMEM_ELEMS);
+        typedef typename cpart<V>::type P;
+        P* mine = reinterpret_cast<P*>(aw_smem + sizeof(V) * Tile::SMEM_ELEMS);
         for (int k = lo + tid; k < hi; k += NT) {
-          double sr = 0.0, si = 0.0;
-          for (int q = 0; q < ncl; ++q) {
-            const double2 v = cl.map_shared_rank(mine, q)[k];
-            sr += v.x;
-            si += v.y;
-          }
-          a.alt_cross[((long long)inst * (gridDim.x / ncl) + blockIdx.x / ncl) * n + k] = make_double2(sr, si);
+          P acc = cpart<V>::zero();
+          for (int q = 0; q < ncl; ++q) acc = cpart<V>::add(acc, cl.map_shared_rank(mine, q)[k]);
+          a.alt_cross[((long long)inst * (gridDim.x / ncl) + blockIdx.x / ncl) * n + k] = cpart<V>::to_d2(acc);
         }
         cl.sync();
       }
