@@ -115,6 +115,15 @@ __device__ __forceinline__ dfr flip(dfr v, unsigned m) { return dfr{flip(v.h, m)
 template <typename V> __device__ __forceinline__ V cflip(V a, unsigned m) { return cmake<V>(flip(a.x, m), flip(a.y, m)); }
 template <typename V> __device__ __forceinline__ V cconj_if(V a, unsigned m) { return cmake<V>(a.x, flip(a.y, m)); }
 
+// butterfly sums: for dfc without renormalisation (cnorm renormalises once at a butterfly's end);
+// the same as cadd / csub for the native types
+template <typename V> __device__ __forceinline__ V cadd_l(V a, V b) { return cadd(a, b); }
+template <typename V> __device__ __forceinline__ V csub_l(V a, V b) { return csub(a, b); }
+template <typename V> __device__ __forceinline__ V cnorm(V a) { return a; }
+template <> __device__ __forceinline__ dfc cadd_l<dfc>(dfc a, dfc b) { return dfc_add_lazy(a, b); }
+template <> __device__ __forceinline__ dfc csub_l<dfc>(dfc a, dfc b) { return dfc_sub_lazy(a, b); }
+template <> __device__ __forceinline__ dfc cnorm<dfc>(dfc a) { return dfc_renorm(a); }
+
 // Transform direction of the FFT helpers: inv = 0 for the forward transform (exp(-i ...)),
 // 0x80000000 for the inverse; the direction is a run-time value so that one copy of the code
 // serves both.

@@ -45,6 +45,17 @@ __device__ __forceinline__ dfr df_add(dfr a, dfr b) {
 }
 
 __device__ __forceinline__ dfr df_neg(dfr a) { return dfr{-a.h, -a.l}; }
+
+// Sum without the final renormalisation (8 instead of 11 instructions): the pair (s, e + a.l + b.l)
+// represents a + b to the same accuracy but its low part may exceed ulp(s) / 2.  A chain of such sums
+// inside one butterfly is renormalised once at its end (df_renorm).
+__device__ __forceinline__ dfr df_add_lazy(dfr a, dfr b) {
+  float s, e;
+  df_two_sum(a.h, b.h, s, e);
+  return dfr{s, e + (a.l + b.l)};
+}
+__device__ __forceinline__ dfr df_sub_lazy(dfr a, dfr b) { return df_add_lazy(a, df_neg(b)); }
+__device__ __forceinline__ dfr df_renorm(dfr a) { return df_fast_two_sum(a.h, a.l); }
 __device__ __forceinline__ dfr df_sub(dfr a, dfr b) { return df_add(a, df_neg(b)); }
 
 __device__ __forceinline__ dfr df_mul(dfr a, dfr b) {
@@ -97,3 +108,6 @@ __device__ __forceinline__ dfc dfc_mulc(dfc a, dfc b) {
   return dfc{df_mul_add(a.x, b.x, a.y, b.y), df_mul_sub(a.y, b.x, a.x, b.y)};
 }
 __device__ __forceinline__ dfc dfc_scale(dfc a, dfr s) { return dfc{df_mul(a.x, s), df_mul(a.y, s)}; }
+__device__ __forceinline__ dfc dfc_add_lazy(dfc a, dfc b) { return dfc{df_add_lazy(a.x, b.x), df_add_lazy(a.y, b.y)}; }
+__device__ __forceinline__ dfc dfc_sub_lazy(dfc a, dfc b) { return dfc{df_sub_lazy(a.x, b.x), df_sub_lazy(a.y, b.y)}; }
+__device__ __forceinline__ dfc dfc_renorm(dfc a) { return dfc{df_renorm(a.x), df_renorm(a.y)}; }

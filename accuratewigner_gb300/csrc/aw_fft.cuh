@@ -57,24 +57,30 @@ __device__ __forceinline__ void split_item(int u, int& line, int& b) {
 // inv: 0 forward, 0x80000000 inverse (sign-bit mask, see aw_common.cuh)
 template <int R, typename V> struct Dft;
 
+// run: outputs renormalised (double-float); run_lazy: sums left unrenormalised for an enclosing butterfly
 template <typename V> struct Dft<2, V> {
   __device__ __forceinline__ static void run(V* v, unsigned) {
     V a = v[0], b = v[1];
-    v[0] = cadd(a, b);
-    v[1] = csub(a, b);
+    v[0] = cnorm(cadd_l(a, b));
+    v[1] = cnorm(csub_l(a, b));
   }
 };
 
 template <typename V> struct Dft<4, V> {
+  __device__ __forceinline__ static void run_lazy(V* v, unsigned inv) {
+    V t0 = cadd_l(v[0], v[2]);
+    V t1 = csub_l(v[0], v[2]);
+    V t2 = cadd_l(v[1], v[3]);
+    V t3 = cmul_mi_dir(csub_l(v[1], v[3]), inv);
+    v[0] = cadd_l(t0, t2);
+    v[2] = csub_l(t0, t2);
+    v[1] = cadd_l(t1, t3);
+    v[3] = csub_l(t1, t3);
+  }
   __device__ __forceinline__ static void run(V* v, unsigned inv) {
-    V t0 = cadd(v[0], v[2]);
-    V t1 = csub(v[0], v[2]);
-    V t2 = cadd(v[1], v[3]);
-    V t3 = cmul_mi_dir(csub(v[1], v[3]), inv);
-    v[0] = cadd(t0, t2);
-    v[2] = csub(t0, t2);
-    v[1] = cadd(t1, t3);
-    v[3] = csub(t1, t3);
+    run_lazy(v, inv);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = cnorm(v[q]);
   }
 };
 
@@ -85,18 +91,18 @@ template <typename V> struct Dft<8, V> {
     V b[4], c[4];
 #pragma unroll
     for (int n = 0; n < 4; ++n) {
-      b[n] = cadd(v[n], v[n + 4]);
-      c[n] = csub(v[n], v[n + 4]);
+      b[n] = cadd_l(v[n], v[n + 4]);
+      c[n] = csub_l(v[n], v[n + 4]);
     }
     c[1] = cmul_w8_1_dir(c[1], inv);
     c[2] = cmul_mi_dir(c[2], inv);
     c[3] = cmul_w8_3_dir(c[3], inv);
-    Dft<4, V>::run(b, inv);
-    Dft<4, V>::run(c, inv);
+    Dft<4, V>::run_lazy(b, inv);
+    Dft<4, V>::run_lazy(c, inv);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      v[2 * q] = b[q];
-      v[2 * q + 1] = c[q];
+      v[2 * q] = cnorm(b[q]);
+      v[2 * q + 1] = cnorm(c[q]);
     }
   }
 };

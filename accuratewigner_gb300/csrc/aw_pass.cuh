@@ -61,17 +61,24 @@ __device__ __forceinline__ void apply_factor(V* r, const AwFactor& f, int lg, in
   if (ct) ct += tab_off;
   if (rt) rt += tab_off;
   if (mk) mk += elem_off;
-  double scr = f.scale, sci = 0.0;
-  if (f.scale_ptr) {
-    scr = f.scale * f.scale_ptr[2 * inst];
-    sci = f.scale * f.scale_ptr[2 * inst + 1];
-  }
   // every factor that depends only on the line, folded into one complex constant:
   //   row tile: conj(row_tab[line]) * scale,  column tile: col_tab[line] * scale
-  V c = cmake<V>(from_double<T>(scr), from_double<T>(sci));
+  // (the FP64 scale is converted only when there is one: conversions run at the FP64 rate)
   const V* lt = Tile::IS_ROW ? rt : ct;
-  if (lt) c = Tile::IS_ROW ? cmulc(c, lt[lg]) : cmul(c, lt[lg]);
-  const bool have_c = lt || scr != 1.0 || sci != 0.0;
+  const bool scaled = f.scale_ptr || f.scale != 1.0;
+  V c;
+  if (scaled) {
+    double scr = f.scale, sci = 0.0;
+    if (f.scale_ptr) {
+      scr = f.scale * f.scale_ptr[2 * inst];
+      sci = f.scale * f.scale_ptr[2 * inst + 1];
+    }
+    c = cmake<V>(from_double<T>(scr), from_double<T>(sci));
+    if (lt) c = Tile::IS_ROW ? cmulc(c, lt[lg]) : cmul(c, lt[lg]);
+  } else if (lt) {
+    c = Tile::IS_ROW ? cconj_if(lt[lg], 0x80000000u) : lt[lg];
+  }
+  const bool have_c = lt || scaled;
   const V* et = Tile::IS_ROW ? ct : rt;  // table along the line
   const int lo_n = f.sh_lo_n;
   const int nhi = lo_n ? Tile::N / lo_n : 0;
@@ -217,7 +224,7 @@ __global__ void __launch_bounds__(NT, (NT <= 128 ? 4 : (NT <= 256 ? 2 : 1))) aw_
     // per-thread partials over the thread's E elements of its column (working precision), then
     // FP64 across threads in a fixed order
     if (a.col_alt || a.alt_cross) {
-      __shared__ double2 cred[NT];
+      __shared__ typename cpart<V>::type cred[NT];
       T cr = from_double<T>(0.0), ci = from_double<T>(0.0);
 #pragma unroll
       for (int k = 0; k < E; ++k) {
@@ -248,15 +255,12 @@ __global__ void __launch_bounds__(NT, (NT <= 128 ? 4 : (NT <= 256 ? 2 : 1))) aw_
         }
       }
       if (a.col_alt) {
-        cred[tid] = make_double2(to_d(cr), to_d(ci));
+        cred[tid] = cpart<V>::make(cr, ci);
         __syncthreads();
         if (tid < B) {
-          double sr = 0.0, si = 0.0;
-          for (int m = tid; m < NT; m += B) {
-            sr += cred[m].x;
-            si += cred[m].y;
-          }
-          a.col_alt[(long long)inst * ncols + line0 + tid] = make_double2(sr, si);
+          typename cpart<V>::type acc = cpart<V>::zero();
+          for (int m = tid; m < NT; m += B) acc = cpart<V>::add(acc, cred[m]);
+          a.col_alt[(long long)inst * ncols + line0 + tid] = cpart<V>::to_d2(acc);
         }
         __syncthreads();
       }
