@@ -14,6 +14,10 @@ when memory is needed.
 Every request's computation is independent of the others in its pool, so a result is the same
 alone and in a mix up to the rounding of its chunk boundaries (a chunk ends with the state
 normalised, as propagate() does).
+
+Precision: an engine runs every request in complex128 ("c128"), in complex64 ("c64"), or picks per
+request ("auto"): complex64 when the error model below keeps the request's relative L2 error within
+its tolerance, complex128 (the FP64-accurate form) otherwise.
 """
 import collections
 import threading
@@ -39,6 +43,18 @@ INIT = {
 CLASSES = {"wm": WignerMoyalCUDA1D, "vn": RhoVNeumannCUDA1D, "rb": RhoBlochCUDA1D}
 
 
+# Relative L2 error of a complex64 propagation after `steps` steps on an n x n grid, against the FP64
+# result: the FP32 rounding of each FFT stage of the 4 propagation transforms a step adds up like a
+# random walk, err = C eps32 sqrt(4 steps log2 n).  C = 3 bounds the measured values (C1, 256^2,
+# 1000 steps: 1.4e-5, C = 1.3; strong-field 1024^2, 1000 steps: 3.2e-5, C = 2.7).
+C64_ERROR_C = 3.0
+EPS32 = 2.0 ** -24
+
+
+def c64_error(n, steps):
+    return C64_ERROR_C * EPS32 * np.sqrt(4.0 * steps * np.log2(n))
+
+
 def amplitude(n):
     """Grid amplitude of side n: dX dP = 2 pi / n with X_amplitude = P_amplitude."""
     return float(np.sqrt(np.pi * n / 2.0))
@@ -48,8 +64,10 @@ class Request:
     """One propagation: kind 'wm' (real-time Wigner-Moyal with Ehrenfest observables), 'vn'
     (real-time von Neumann) or 'rb' (rho-Bloch Gibbs state after `steps` steps of dbeta)."""
 
-    def __init__(self, rid, kind, n, steps, coeffs, x0=0.0, p0=0.0, arrival=0.0, keep_state=False):
+    def __init__(self, rid, kind, n, steps, coeffs, x0=0.0, p0=0.0, arrival=0.0, keep_state=False, tol=1e-5):
         self.rid = rid
+        self.tol = float(tol)    # relative L2 error the request accepts ("auto" engines)
+        self.precision = None    # the form it ran in
         self.kind = kind
         self.n = int(n)
         self.steps = int(steps)
@@ -193,6 +211,7 @@ class Engine:
     """Continuous-batching request loop on one GPU."""
 
     def __init__(self, precision="c128", chunk=200, dt=0.01, dbeta=0.01, slots=None, reserve_bytes=2 << 30):
+        assert precision in ("c128", "c64", "auto", "c128-fp64")
         self.precision = precision
         self.chunk = chunk
         self.dt = dt
@@ -212,14 +231,20 @@ class Engine:
         free, _ = torch.cuda.mem_get_info()
         return free
 
-    def pool(self, kind, n):
-        """The pool of (kind, n), created when the free device memory covers it."""
-        key = (kind, n)
+    def precision_for(self, req):
+        if self.precision != "auto":
+            return self.precision
+        return "c64" if c64_error(req.n, req.steps) <= req.tol else "c128"
+
+    def pool(self, kind, n, precision=None):
+        """The pool of (kind, n, precision), created when the free device memory covers it."""
+        precision = precision or (self.precision if self.precision != "auto" else "c128")
+        key = (kind, n, precision)
         with self.lock:
             p = self.pools.get(key)
             if p is not None:
                 return p
-            need = pool_bytes(kind, n, self.slots[n]) + self.reserve
+            need = pool_bytes(kind, n, self.slots[n]) // (2 if precision == "c64" else 1) + self.reserve
             while self._free_bytes() < need:
                 # release an idle pool, or wait for one to become idle
                 idle = [k for k, q in self.pools.items() if q.idle()]
@@ -229,22 +254,25 @@ class Engine:
                     q.join()
                     continue
                 if not self.pools:
-                    raise MemoryError("not enough device memory for a %s pool of side %d" % key)
+                    raise MemoryError("not enough device memory for a %s pool of side %d (%s)" % key)
                 time.sleep(0.01)
-            p = Pool(self, kind, n, self.slots[n], self.precision, self.chunk, self.dt, self.dbeta)
+            p = Pool(self, kind, n, self.slots[n], precision, self.chunk, self.dt, self.dbeta)
             self.pools[key] = p
             p.start()
             return p
 
     def warm(self, kinds=("wm", "vn", "rb"), sides=(128, 256, 512, 1024, 2048)):
         """Create the pools ahead of the first request (JIT compile, buffers), as a server starts."""
+        precs = ("c128", "c64") if self.precision == "auto" else (self.precision,)
         for k in kinds:
             for n in sides:
-                self.pool(k, n)
+                for p in precs:
+                    self.pool(k, n, p)
 
     # requests ---------------------------------------------------------------
     def submit(self, req):
-        self.pool(req.kind, req.n).submit(req)
+        req.precision = self.precision_for(req)
+        self.pool(req.kind, req.n, req.precision).submit(req)
 
     def _finished(self, req):
         with self.done_cv:

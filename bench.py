@@ -20,6 +20,8 @@ Other workloads (one JSON line each, not the headline):
   --workload served         Poisson stream of Wigner-Moyal / von Neumann / rho-Bloch requests through
                             the continuous-batching loop: p50 / p99 latency and aggregate throughput
   --workload large-vn       von Neumann 4096 x 4096, driven Morse potential, 2000 steps
+  --workload precision      the headline workload in complex128 (double-float), complex64 and native
+                            FP64 side by side: errors of W and of <x>, <p>, dipole acceleration per step
 """
 import argparse
 import ctypes
@@ -75,7 +77,8 @@ CHUNK = 50  # steps per propagate() call, as the reference's own driver loop (wi
 
 STATE_BYTES_PER_PT = {"c128": 16, "c128-fp64": 16, "c64": 8}
 # arithmetic of the passes per precision
-DTYPE = {"c128": "c128 state, f32x2 double-float arithmetic", "c128-fp64": "f64", "c64": "f32+f64"}
+DTYPE = {"c128": "c128 state, f32x2 double-float arithmetic", "c128-fp64": "f64", "c64": "f32+f64",
+         "auto": "per request: c64 (f32+f64) within the error bound, else c128"}
 ALG_BYTES_FACTOR = 10  # bytes per grid point per step = 10 * S (propagation 4 S + per-step Wigner transform 6 S)
 
 
@@ -454,6 +457,42 @@ def run_batched_gibbs(args):
            "precision": args.precision}, extra)
 
 
+def run_precision(args):
+    """The headline workload run in native FP64 (the reference), double-float complex128 and complex64:
+    relative L2 error of W every 50 steps and the largest error of <x>, <p> and the dipole
+    acceleration over the steps."""
+    from accuratewigner_gb300 import WignerMoyalCUDA1D
+
+    steps = args.steps if args.steps != 200 else 1000
+    w0 = make_propagator("c128").wignerfunction.get()
+
+    def run(prec):
+        g = WignerMoyalCUDA1D(**PARAMS, precision=prec)
+        g.set_wignerfunction(w0)
+        ws = []
+        for _ in range(steps // CHUNK):
+            g.propagate(CHUNK)
+            ws.append(g.wignerfunction.get())
+        obs = {k: np.array(getattr(g, k)) for k in ("X_average", "P_average", "P_average_RHS")}
+        g._handle.close()
+        return ws, obs
+
+    ref_w, ref_o = run("c128-fp64")
+    out = {}
+    for prec in ("c128", "c64"):
+        ws, obs = run(prec)
+        w_err = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(ws, ref_w)]
+        o_err = {k: float(np.max(np.abs(obs[k] - ref_o[k]) / np.maximum(np.abs(ref_o[k]), 1.0))) for k in obs}
+        out[prec] = {"W_rel_l2_every_50_steps": w_err, "W_rel_l2_final": w_err[-1],
+                     "max_scaled_err": {"x": o_err["X_average"], "p": o_err["P_average"],
+                                        "dipole_acceleration": o_err["P_average_RHS"]}}
+    _line("precision", "relative L2 error of W vs native FP64 after %d steps (c64)" % steps,
+          out["c64"]["W_rel_l2_final"], "relative L2", 0.0, args,
+          {"workload": "strong-field Wigner-Moyal 1024x1024 (the headline)", "steps": steps,
+           "reference": "c128-fp64 (native FP64 passes)", "observable_scale": "max(|ref|, 1)"},
+          {"errors": out}, higher=False)
+
+
 def run_served(args):
     """Poisson stream of Wigner-Moyal / von Neumann / rho-Bloch requests, sides {128 .. 2048},
     steps ~ U(100, 5000), through the continuous-batching request loop."""
@@ -532,16 +571,19 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="c128", choices=["c128", "c128-fp64", "c64"])
+    ap.add_argument("--precision", default="c128", choices=["c128", "c128-fp64", "c64", "auto"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="strong-field",
-                    choices=["strong-field", "plain", "batched-gibbs", "served", "large-vn"])
+                    choices=["strong-field", "plain", "batched-gibbs", "served", "large-vn", "precision"])
     ap.add_argument("--requests", type=int, default=60, help="served: number of requests")
-    ap.add_argument("--rate", type=float, default=1.2, help="served: Poisson arrival rate per second")
+    ap.add_argument("--rate", type=float, default=4.0, help="served: Poisson arrival rate per second")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    other = {"plain": run_plain, "batched-gibbs": run_batched_gibbs, "served": run_served, "large-vn": run_large_vn}
+    other = {"plain": run_plain, "batched-gibbs": run_batched_gibbs, "served": run_served, "large-vn": run_large_vn,
+             "precision": run_precision}
+    if args.precision == "auto" and args.workload != "served":
+        ap.error("--precision auto chooses per request: only the served workload has requests")
     if args.workload in other:
         import torch
 

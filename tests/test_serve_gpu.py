@@ -63,3 +63,23 @@ def test_served_wigner_moyal_matches_the_plain_propagator():
     assert rel_l2(r.state, s.wignerfunction.get()) < 1e-10
     h = np.concatenate(r.history)
     assert obs_close(h[:, 0], s.X_average, 1e-10)
+
+
+def test_auto_precision_meets_each_request_tolerance():
+    from accuratewigner_gb300.serve import Engine, Request
+
+    def reqs():
+        return [Request(0, "wm", 64, 30, (0.5, 0.01, 0.02), 0.5, -0.3, keep_state=True, tol=1e-5),
+                Request(1, "vn", 64, 400, (0.3, 0.0, 0.01), -0.7, 0.4, keep_state=True, tol=1e-9)]
+
+    auto = reqs()
+    eng = Engine(precision="auto", chunk=50, slots={64: 2})
+    eng.run(auto, realtime=False)
+    eng.close()
+    ref = reqs()
+    e2 = Engine(precision="c128", chunk=50, slots={64: 2})
+    e2.run(ref, realtime=False)
+    e2.close()
+    assert auto[0].precision == "c64" and auto[1].precision == "c128"
+    for a, r in zip(auto, ref):
+        assert rel_l2(a.state, r.state) <= a.tol, (a.rid, rel_l2(a.state, r.state))

@@ -28,3 +28,17 @@ def test_pool_memory_grows_with_side_and_slots():
     for n in (128, 2048):
         a = amplitude(n)
         assert abs((2 * a / n) ** 2 - 2 * np.pi / n) < 1e-12
+
+
+def test_auto_precision_routes_by_the_error_model():
+    from accuratewigner_gb300.serve import Engine, Request, c64_error
+
+    eng = Engine(precision="auto")
+    short = Request(0, "wm", 128, 50, (0.5, 0.0, 0.0), tol=1e-5)
+    long = Request(1, "wm", 2048, 5000, (0.5, 0.0, 0.0), tol=1e-5)
+    loose = Request(2, "vn", 2048, 5000, (0.5, 0.0, 0.0), tol=1e-3)
+    assert c64_error(128, 50) <= 1e-5 < c64_error(2048, 5000) <= 1e-3
+    assert eng.precision_for(short) == "c64"
+    assert eng.precision_for(long) == "c128"
+    assert eng.precision_for(loose) == "c64"
+    assert Engine(precision="c128").precision_for(short) == "c128"
