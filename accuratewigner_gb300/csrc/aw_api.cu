@@ -184,7 +184,6 @@ struct aw_state_s {
   int twist_lo_n = 0;
   int sw_rows = 1;                     // Schrodinger: rows of the zero-padded psi tile
   int red_blocks = 0;                  // column blocks of the Wigner column pass
-  int row_blocks = 0;                  // row blocks of the main row pass
   long long hist_rows = 0, hist_cap = 0;
   int hist_cols = 0;
   double V_min = 0.0, K_min = 0.0;
@@ -236,6 +235,12 @@ static double* dtv(aw_state_s* h, int inst) { return (double*)h->scal.p + 2 * h-
 static int* dstop(aw_state_s* h, int inst = 0) { return (int*)h->stop.p + inst; }
 static unsigned int* dcounter(aw_state_s* h, int inst) { return (unsigned int*)h->stop.p + h->ni + inst; }
 static long long gsz(const aw_state_s* h) { return (long long)h->nr * h->nc; }
+// rows per row-pass block and row-pass blocks per instance for a grid of nrows x ncols: chosen from
+// the rows of all instances of the handle, so that every launch of a batch splits rows the same way
+static int row_lines(const aw_state_s* h, int nrows, int ncols) {
+  return aw_row_pass_lines_for(nrows * h->ni, ncols, h->f32);
+}
+static int row_blocks(const aw_state_s* h, int nrows, int ncols) { return nrows / row_lines(h, nrows, ncols); }
 static void* at_inst(void* base, long long elems, int esz, int inst) {
   return base ? (char*)base + (size_t)inst * elems * esz : nullptr;
 }
@@ -528,6 +533,7 @@ static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row)
     if (!a.stop) a.stop = dstop(h);
     if (!row && !a.lines_hint) a.lines_hint = h->col_lines;
   }
+  if (row && !a.row_lines) a.row_lines = row_lines(h, a.nrows, a.ncols);
   if (h->df) TRY(df_prepare(h, a, batch));
   cudaEvent_t pe = prof_mark(h);
   int r;
@@ -1346,7 +1352,7 @@ static int launch_finalize_rot(aw_state_s* h, double t, double* hist_row, int st
   // every instance of the view: blockIdx.y = instance - v0
   const int i0 = h->v0;
   int nparts = h->z_blocks;
-  int nb2 = aw_row_pass_blocks(h->nr, h->nc, h->f32);
+  int nb2 = row_blocks(h, h->nr, h->nc);
   const double2* z = zbuf_of(h, par) + (size_t)i0 * h->nc;
   const double2* wpart = altbuf_of(h, par) + (size_t)i0 * nparts * h->nr;
   const double* abs2 = abs2_of(h, par) + (size_t)i0 * nb2;
@@ -1922,7 +1928,7 @@ static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::ve
   TRY(vinv_reset(h));
   TRY(reset_stops(h));  // a stop raised by an earlier call must not persist
   const int* stop = p.stop_on_purity || h->ni > 1 ? (const int*)dstop(h) : nullptr;
-  const int row_blocks = aw_row_pass_blocks(h->nr, h->nc, h->f32);
+  const int nrb = row_blocks(h, h->nr, h->nc);
   const int vslot = p.bloch ? TAB_BV : TAB_V1;
   const int kslot = p.bloch ? TAB_BK : TAB_K;
   // for time-dependent V the next step's kick needs its own table
@@ -1998,7 +2004,7 @@ static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::ve
     }
     if (p.bloch || !p.observables) {
       KL(aw_k_trace_finalize_n((const double2*)h->diag.p + (size_t)h->v0 * N,
-                               N, (const double*)h->abs2.p + (size_t)h->v0 * row_blocks, row_blocks, c.dX,
+                               N, (const double*)h->abs2.p + (size_t)h->v0 * nrb, nrb, c.dX,
                                p.complex_trace, dinv(h, h->v0), p.observables ? nullptr : hrow, inst_stride,
                                dstop(h, h->v0), p.stop_on_purity, h->vc, h->st));
     }
@@ -2038,7 +2044,7 @@ int vn_bloch_step(aw_state_s* h, double dbeta, double* out) {
   TRY(vn_run(h, p, 1, times, (double*)h->hist.p, h->hist_cols));
   if (obs)
     KL(aw_k_trace_finalize((const double2*)h->diag.p, h->nc, (const double*)h->abs2.p,
-                           aw_row_pass_blocks(h->nr, h->nc, h->f32), h->cfg.dX, 1, dmisc(h, 0),
+                           row_blocks(h, h->nr, h->nc), h->cfg.dX, 1, dmisc(h, 0),
                            (double*)h->hist.p + h->hist_cols, nullptr, 0, h->st));
   TRY(settle(h));
   TRY(vscale(h, h->rho.p, gsz(h)));
@@ -2228,7 +2234,7 @@ int sw_propagate(aw_state_s* h, long long steps, double* t) {
   const bool tdep = c.v_time_dependent || c.k_time_dependent || c.absx_mode == 2 || c.absp_mode == 2;
   KL(aw_k_set2(dinv(h), 1.0, 0.0, h->st));
   if (!tdep) TRY(sw_tables(h, times[1]));
-  const int nb = aw_row_pass_blocks(h->sw_rows, h->nc, h->f32);
+  const int nb = row_blocks(h, h->sw_rows, h->nc);
   for (long long n = 1; n <= steps; ++n) {
     if (tdep) TRY(sw_tables(h, times[n]));
     AwPassArgs a = sw_args(h);
@@ -2323,7 +2329,7 @@ extern "C" int aw_sw_imag_steps(aw_handle h, int64_t steps, int32_t project) {
   // bloch_expV = exp(-dt/2 V(X, t_initial)), bloch_expK = exp(-dt K(P, t_initial))  (sw:834-854)
   TRY(build_tab(h, TAB_BV, 0, 1, c.t_initial, 0.0, -0.5 * c.dt, 0.0, 0.0, 0, 0.0));
   TRY(build_tab(h, TAB_BK, 1, 1, c.t_initial, 0.0, -c.dt, 0.0, 0.0, 0, 0.0));
-  const int nb = aw_row_pass_blocks(h->sw_rows, h->nc, h->f32);
+  const int nb = row_blocks(h, h->sw_rows, h->nc);
   const int N = h->nc;
   for (long long n = 0; n < steps; ++n) {
     AwPassArgs a = sw_args(h);

@@ -326,6 +326,14 @@ inline int choose_row_lines(int ncols, int esz) {
   return l;
 }
 
+// rows per row-pass block for a grid of nrows rows: tiles of about 1024 elements, or one row a
+// block when that would leave fewer than two blocks per SM (small grids; not the zero-padded tile
+// of a wave function, whose nrows equals the tile)
+inline int choose_row_lines(int nrows, int ncols, int esz) {
+  const int l = choose_row_lines(ncols, esz);
+  return (l > 1 && nrows > l && nrows / l < 2 * AW_SMS) ? 1 : l;
+}
+
 // columns per column-pass block: as many as fit (<= 16, <= 128 KB of shared memory, <= 512
 // threads so that the 16-byte element types keep their registers)
 inline int max_col_lines(int nrows, int ncols, int esz) {
@@ -411,7 +419,11 @@ static int launch_col_t(const AwPassArgs* a, int batch, cudaStream_t st) {
 
 template <typename V, int N> static int launch_row_n(const AwPassArgs* a, int batch, cudaStream_t st) {
   constexpr int L = 1024 / N >= 1 ? 1024 / N : 1;
-  return launch_row_t<V, N, L>(a, batch, st);
+  const int l = a->row_lines ? a->row_lines : choose_row_lines(a->nrows, N, (int)sizeof(V));
+  if constexpr (L > 1) {
+    if (l == 1) return launch_row_t<V, N, 1>(a, batch, st);
+  }
+  return l == L ? launch_row_t<V, N, L>(a, batch, st) : -7;
 }
 
 template <typename V, int N> static int launch_col_n(const AwPassArgs* a, int batch, cudaStream_t st) {

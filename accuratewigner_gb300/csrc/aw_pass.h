@@ -67,6 +67,7 @@ typedef struct AwPassArgs {
   long long batch_elems;    // batched launches: elements per instance (blockIdx.y)
   long long batch_tab;      // ... table entries per instance
   int inst0;                // instance of blockIdx.y = 0 (a launch over a range of a batch's instances)
+  int row_lines;            // row pass: rows per block (0: chosen from nrows)
 } AwPassArgs;
 
 // Host-side launchers, one per precision (aw_pass_f64.cu / aw_pass_f32.cu).
@@ -82,6 +83,8 @@ int aw_col_pass_blocks(int nrows, int ncols, int f32);
 // columns per column-pass block for `batch` instances
 int aw_col_pass_lines(int nrows, int ncols, int batch, int f32);
 // the most columns a column-pass block can hold (shared-memory limit)
+// rows per row-pass block for a launch covering `rows_total` rows of length ncols (all instances)
+int aw_row_pass_lines_for(int rows_total, int ncols, int f32);
 int aw_col_pass_max_lines(int nrows, int ncols, int f32);
 // number of rows one row-pass block holds for a row length ncols
 int aw_row_pass_lines(int ncols, int f32);
