@@ -207,13 +207,12 @@ def run_ours(args):
             times.append(e0.elapsed_time(e1) / 1e3)
     torch.cuda.synchronize()
     launches = _lib.launch_count() - launches0
-    total = float(sum(times))
+    from accuratewigner_gb300.replicas import job_throughput
+
+    # replicas: the slowest rank's time, the work of all ranks
+    total, _, value = job_throughput(float(sum(times)), npts * args.steps, device="cuda")
     if dist:
-        tt = torch.tensor([total], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total = float(tt.item())
         dist.barrier()
-    value = npts * args.steps * world / total
 
     # per-kernel timing of one chunk (separate run, events around every launch)
     _lib.check(lib.aw_profile(h, 1))
@@ -250,12 +249,7 @@ def run_ours(args):
         _ = prop.X_average[-n:], prop.P_average[-n:], prop.P_average_RHS[-n:]
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
-    e2e_total = float(sum(e2e_times))
-    if dist:
-        tt = torch.tensor([e2e_total], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_total = float(tt.item())
-    e2e_value = npts * args.steps * world / e2e_total
+    e2e_total, _, e2e_value = job_throughput(float(sum(e2e_times)), npts * args.steps, device="cuda")
     S = STATE_BYTES_PER_PT[args.precision]
     h2d = npts * 16 * len(chunks) / args.steps
     d2h = (npts * 16 + CHUNK * 7 * 8) * len(chunks) / args.steps
