@@ -16,8 +16,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <unordered_map>
 #include <vector>
 
@@ -149,6 +151,7 @@ struct aw_state_s {
   std::vector<char> minima_ok;
   int col_lines = 0;                   // columns per column-pass block of a batch (fixed, so that an
                                        // instance computes the same way whatever the view)
+  int tuned_col_lines = 0;             // ... of the propagation column pass, chosen by timing (tune_col_lines)
   cudaKernel_t k_binit = nullptr;
   // buffers currently holding double-float state (pointer, elements); plain complex128 at rest
   std::vector<std::pair<void*, long long>> df_live;
@@ -633,6 +636,74 @@ extern "C" int64_t aw_launch_count(void) { return g_launches.load(); }
 
 static std::string cstr(const char* s, const char* dflt) { return s ? std::string(s) : std::string(dflt); }
 
+// ============================================================================ tile autotuner
+// Columns per block of the propagation column pass (ifft0, phase multiply, fft0), chosen by timing
+// every candidate once per (grid, instances, form) in this process.  Wider blocks coalesce the
+// strided column loads better, narrower ones put more blocks on the SMs; which wins depends on the
+// grid, the batch and the arithmetic form.  The pass has no reductions and every column is
+// transformed by the same operations whatever the block width, so the choice never changes a result.
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int, int>, int> g_tuned;
+
+static AwFactor fshear_y(aw_state_s* h);
+
+static int tune_col_lines(aw_state_s* h) {
+  if (h->kn.sw) return AW_OK;
+  const auto key = std::make_tuple(h->nr, h->nc, h->ni, h->df ? 2 : (h->f32 ? 1 : 0));
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      h->tuned_col_lines = it->second;
+      return AW_OK;
+    }
+  }
+  const int bmax = aw_col_pass_max_lines(h->nr, h->nc, h->f32);
+  std::vector<int> cand;
+  for (int b = 1; b <= bmax; b *= 2) cand.push_back(b);
+  int best = cand.empty() ? 1 : cand[0];
+  if (cand.size() > 1) {
+    CK(cudaMemsetAsync(h->tmp.p, 0, (size_t)h->ni * gsz(h) * h->esz, h->st));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best_ms = 0.f;
+    for (int b : cand) {
+      AwPassArgs a = pnone(h);
+      a.in = a.out = h->tmp.p;
+      a.d1 = -1;
+      a.f1 = fshear_y(h);  // a table read and two complex multiplies per point, as a phase kick
+      a.d2 = +1;
+      a.lines_hint = b;
+      int r = col_pass(h, a, h->tw_c);  // warm-up (first launch of this instantiation)
+      float ms = 0.f;
+      if (!r) {
+        cudaEventRecord(e0, h->st);
+        for (int k = 0; k < 3 && !r; ++k) r = col_pass(h, a, h->tw_c);
+        cudaEventRecord(e1, h->st);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+      }
+      if (r) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return r;
+      }
+      if (b == cand[0] || ms < best_ms) {
+        best_ms = ms;
+        best = b;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    TRY(settle(h));
+  }
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tuned[key] = best;
+  h->tuned_col_lines = best;
+  return AW_OK;
+}
+
 // Bloch minima of instance i: min over (V(x) + V(x')) = min V(x) + min V(x') since rounding is
 // monotone (the reference's V_min / K_min, wigner_bloch_cuda_1d.py:55-92)
 static int bloch_minima(aw_state_s* h, int i) {
@@ -902,6 +973,8 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
     if (cfg->absx_mode) TRY(dalloc(h->maskx, ni * grid * (h->f32 ? 4 : 8)));
     if (cfg->absp_mode) TRY(dalloc(h->maskp, ni * grid * (h->f32 ? 4 : 8)));
   }
+
+  TRY(tune_col_lines(h));
 
   if (h->kind == AW_WIGNER_BLOCH || h->kind == AW_RHO_BLOCH) {
     // minima of every instance (a batch recomputes an instance's after aw_set_params)
@@ -1605,6 +1678,7 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       }
       a.d2 = +1;
       a.stop = stop;
+      a.lines_hint = h->tuned_col_lines;
       TRY(col_pass(h, a, h->tw_c));
     }
     // row pass: ifft1, V-kick(t_n) [branch: Wigner transform] [next kick(t_{n+1}), fft1 | S]
@@ -1956,6 +2030,7 @@ static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::ve
       a.f1 = ftab(h, kslot);
       a.d2 = +1;
       a.stop = stop;
+      a.lines_hint = h->tuned_col_lines;
       TRY(col_pass(h, a, h->tw_c));
     }
     {
