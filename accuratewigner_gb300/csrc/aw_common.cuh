@@ -123,6 +123,11 @@ template <typename V> __device__ __forceinline__ V cnorm(V a) { return a; }
 template <> __device__ __forceinline__ dfc cadd_l<dfc>(dfc a, dfc b) { return dfc_add_lazy(a, b); }
 template <> __device__ __forceinline__ dfc csub_l<dfc>(dfc a, dfc b) { return dfc_sub_lazy(a, b); }
 template <> __device__ __forceinline__ dfc cnorm<dfc>(dfc a) { return dfc_renorm(a); }
+// products likewise: for dfc without renormalisation
+template <typename V> __device__ __forceinline__ V cmul_l(V a, V b) { return cmul(a, b); }
+template <typename V> __device__ __forceinline__ V cmulc_l(V a, V b) { return cmulc(a, b); }
+template <> __device__ __forceinline__ dfc cmul_l<dfc>(dfc a, dfc b) { return dfc_mul_lazy(a, b); }
+template <> __device__ __forceinline__ dfc cmulc_l<dfc>(dfc a, dfc b) { return dfc_mulc_lazy(a, b); }
 
 // Transform direction of the FFT helpers: inv = 0 for the forward transform (exp(-i ...)),
 // 0x80000000 for the inverse; the direction is a run-time value so that one copy of the code

@@ -66,8 +66,9 @@ __device__ __forceinline__ dfr df_mul(dfr a, dfr b) {
   return df_fast_two_sum(p, e);
 }
 
-// a*b - c*d with one renormalisation (the real part of a complex product)
-__device__ __forceinline__ dfr df_mul_sub(dfr a, dfr b, dfr c, dfr d) {
+// a*b - c*d without the final renormalisation (the real part of a complex product): the pair
+// (s, e) represents the result as accurately as its renormalised form, with |e| up to a few ulp(s)
+__device__ __forceinline__ dfr df_mul_sub_lazy(dfr a, dfr b, dfr c, dfr d) {
   const float p1 = __fmul_rn(a.h, b.h);
   const float e1 = __fmaf_rn(a.h, b.h, -p1);
   const float p2 = __fmul_rn(c.h, d.h);
@@ -79,7 +80,12 @@ __device__ __forceinline__ dfr df_mul_sub(dfr a, dfr b, dfr c, dfr d) {
   e = __fmaf_rn(a.l, b.h, e);
   e = __fmaf_rn(-c.h, d.l, e);
   e = __fmaf_rn(-c.l, d.h, e);
-  return df_fast_two_sum(s, e);
+  return dfr{s, e};
+}
+// a*b - c*d with one renormalisation
+__device__ __forceinline__ dfr df_mul_sub(dfr a, dfr b, dfr c, dfr d) {
+  const dfr r = df_mul_sub_lazy(a, b, c, d);
+  return df_fast_two_sum(r.h, r.l);
 }
 
 // a*b + c*d
@@ -108,6 +114,13 @@ __device__ __forceinline__ dfc dfc_mulc(dfc a, dfc b) {
   return dfc{df_mul_add(a.x, b.x, a.y, b.y), df_mul_sub(a.y, b.x, a.x, b.y)};
 }
 __device__ __forceinline__ dfc dfc_scale(dfc a, dfr s) { return dfc{df_mul(a.x, s), df_mul(a.y, s)}; }
+// complex products without the final renormalisation, for chains that end in one (df_renorm)
+__device__ __forceinline__ dfc dfc_mul_lazy(dfc a, dfc b) {
+  return dfc{df_mul_sub_lazy(a.x, b.x, a.y, b.y), df_mul_sub_lazy(a.x, b.y, df_neg(a.y), b.x)};
+}
+__device__ __forceinline__ dfc dfc_mulc_lazy(dfc a, dfc b) {
+  return dfc{df_mul_sub_lazy(a.x, b.x, df_neg(a.y), b.y), df_mul_sub_lazy(a.y, b.x, a.x, b.y)};
+}
 __device__ __forceinline__ dfc dfc_add_lazy(dfc a, dfc b) { return dfc{df_add_lazy(a.x, b.x), df_add_lazy(a.y, b.y)}; }
 __device__ __forceinline__ dfc dfc_sub_lazy(dfc a, dfc b) { return dfc{df_sub_lazy(a.x, b.x), df_sub_lazy(a.y, b.y)}; }
 __device__ __forceinline__ dfc dfc_renorm(dfc a) { return dfc{df_renorm(a.x), df_renorm(a.y)}; }

@@ -136,7 +136,7 @@ __device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __res
     split_item<Tile>(tid + m * NT, line, b);
     const int k = b & (NS - 1);
 #pragma unroll
-    for (int r = 1; r < R; ++r) v[m][r] = cmul(v[m][r], cconj_if(tw[r * k * (N / (NS * R))], inv));
+    for (int r = 1; r < R; ++r) v[m][r] = cmul_l(v[m][r], cconj_if(tw[r * k * (N / (NS * R))], inv));
     Dft<R, V>::run(v[m], inv);
     const int base = (b / NS) * NS * R + k;
 #pragma unroll
@@ -209,7 +209,7 @@ __device__ __forceinline__ void tile_fft_regs(V* r, V* __restrict__ s, const V* 
     split_item<Tile>(tid + m * NT, line, b);
     // b < NSL here, so the twiddle exponent is q * b and the outputs go to b + q * NSL
 #pragma unroll
-    for (int q = 1; q < RL; ++q) v[m][q] = cmul(v[m][q], cconj_if(tw[q * b], inv));
+    for (int q = 1; q < RL; ++q) v[m][q] = cmul_l(v[m][q], cconj_if(tw[q * b], inv));
     Dft<RL, V>::run(v[m], inv);
 #pragma unroll
     for (int q = 0; q < RL; ++q) r[m + q * PERL] = v[m][q];

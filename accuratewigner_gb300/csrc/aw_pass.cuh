@@ -95,14 +95,14 @@ __device__ __forceinline__ void apply_factor(V* r, const AwFactor& f, int lg, in
       if (f.mask_pow == 2) q = q * q;
       v = cscale(v, q);
     }
-    if (et) v = Tile::IS_ROW ? cmul(v, et[j]) : cmulc(v, et[i]);
-    if (have_c) v = cmul(v, c);
+    if (et) v = Tile::IS_ROW ? cmul_l(v, et[j]) : cmulc_l(v, et[i]);
+    if (have_c) v = cmul_l(v, c);
     if (lo_n) {
       const int q = (pos + f.sh_roll) & (Tile::N - 1);
-      V w = cmul(sh[(long long)lg * nhi + q / lo_n], sl[(long long)lg * lo_n + (q % lo_n)]);
-      v = cmul(v, w);
+      V w = cmul_l(sh[(long long)lg * nhi + q / lo_n], sl[(long long)lg * lo_n + (q % lo_n)]);
+      v = cmul_l(v, w);
     }
-    r[k] = v;
+    r[k] = cnorm(v);
   }
 }
 
