@@ -186,6 +186,12 @@ struct aw_state_s {
   DevBuf twist_hi, twist_lo;           // von Neumann momentum-diagonal twist exp(2 pi i k i / N) / N
   int twist_lo_n = 0;
   int sw_rows = 1;                     // Schrodinger: rows of the zero-padded psi tile
+  // Schrodinger wave functions longer than one pass tile: psi read as an sw_n1 x sw_n2 matrix and
+  // transformed by the four-step FFT (sw_run); 0 for the single-tile form
+  int sw_n1 = 0, sw_n2 = 0;
+  DevBuf tw_l1, tw_l2;                 // twiddles of the two factor lengths
+  DevBuf swf_hi, swf_lo, swi_hi, swi_lo;  // exp(-+ 2 pi i n2 k1 / N) between the two stages
+  int swt_lo_n = 0;
   int red_blocks = 0;                  // column blocks of the Wigner column pass
   long long hist_rows = 0, hist_cap = 0;
   int hist_cols = 0;
@@ -430,6 +436,28 @@ static int make_twist(DevBuf& hi, DevBuf& lo, int* lo_n, int n, int fmt) {
       L[2 * ((size_t)ln * LO + l)] = (double)cosl(a);
       L[2 * ((size_t)ln * LO + l) + 1] = (double)sinl(a);
     }
+  }
+  TRY(upload_reals(hi, H, fmt));
+  TRY(upload_reals(lo, L, fmt));
+  *lo_n = LO;
+  return AW_OK;
+}
+
+// exp(sign 2 pi i (line * q mod modulus) / modulus) for lines x npos, split as hi[q / lo] * lo[q % lo]
+// (the four-step FFT's twiddles: line = n2, q = k1, modulus = N), exact integer reduction
+static int make_twist4(DevBuf& hi, DevBuf& lo, int* lo_n, int lines, int npos, long long modulus, int sign, int fmt) {
+  const int LO = npos < 32 ? npos : 32;
+  const int nhi = npos / LO;
+  const long double PI = 3.141592653589793238462643383279502884L;
+  std::vector<double> H(2 * (size_t)lines * nhi), L(2 * (size_t)lines * LO);
+  auto put = [&](std::vector<double>& v, size_t k, long long m) {
+    const long double a = sign * 2.0L * PI * (long double)m / (long double)modulus;
+    v[2 * k] = (double)cosl(a);
+    v[2 * k + 1] = (double)sinl(a);
+  };
+  for (long long ln = 0; ln < lines; ++ln) {
+    for (int hh = 0; hh < nhi; ++hh) put(H, (size_t)ln * nhi + hh, (ln * (long long)(hh * LO)) % modulus);
+    for (int l = 0; l < LO; ++l) put(L, (size_t)ln * LO + l, (ln * (long long)l) % modulus);
   }
   TRY(upload_reals(hi, H, fmt));
   TRY(upload_reals(lo, L, fmt));
@@ -807,10 +835,20 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
     h->nr = 1;
     h->nc = N;
     h->wn = N;
-    h->sw_rows = aw_row_pass_lines(N, h->f32);
-    if (h->sw_rows <= 0) return fail(AW_E_ARG, "unsupported wave-function length %d", N);
+    if (N > 8192) {
+      // longer than one pass tile: an N1 x N2 matrix, N1 <= N2 <= 8192 (no N x N Wigner grid)
+      int n1 = 1;
+      while ((long long)n1 * n1 * 4 <= N) n1 *= 2;
+      h->sw_n1 = n1;
+      h->sw_n2 = N / n1;
+      h->wn = 0;
+      if (h->sw_n2 > 8192) return fail(AW_E_ARG, "wave functions up to 2^25 points");
+    } else {
+      h->sw_rows = aw_row_pass_lines(N, h->f32);
+      if (h->sw_rows <= 0) return fail(AW_E_ARG, "unsupported wave-function length %d", N);
+    }
   }
-  const int maxn = h->kn.sw ? 8192 : 8192;
+  const int maxn = h->kn.sw ? (1 << 25) : 8192;
   if (h->nc < 32 || h->nc > maxn || (!h->kn.sw && (h->nr < 32 || h->nr > maxn)) || (h->wn && h->wn > 8192))
     return fail(AW_E_ARG, "grid sides must be powers of two in [32, %d] (Wigner grid up to 8192)", maxn);
 
@@ -869,7 +907,8 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   // buffers
   const size_t ni = h->ni;
   const size_t grid = (size_t)(h->kn.sw ? h->sw_rows : h->nr) * h->nc;
-  const size_t wgrid = h->kn.rotated ? grid : (size_t)h->wn * h->wn;
+  // Wigner grid; for a long wave function (no Wigner grid) a psi-sized scratch
+  const size_t wgrid = h->kn.rotated ? grid : std::max((size_t)h->wn * h->wn, h->kn.sw ? grid : (size_t)0);
   TRY(dalloc(h->rho, ni * grid * h->esz));
   TRY(dalloc(h->W, ni * wgrid * h->esz));
   TRY(dalloc(h->tmp, std::max(ni * grid, wgrid) * 16));
@@ -904,7 +943,14 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   }
 
   // twiddles
-  TRY(make_twiddles(h->tw_r, h->nc, tab_fmt(h)));
+  if (h->sw_n1) {
+    TRY(make_twiddles(h->tw_l1, h->sw_n1, tab_fmt(h)));
+    TRY(make_twiddles(h->tw_l2, h->sw_n2, tab_fmt(h)));
+    TRY(make_twist4(h->swf_hi, h->swf_lo, &h->swt_lo_n, h->sw_n2, h->sw_n1, N, -1, tab_fmt(h)));
+    TRY(make_twist4(h->swi_hi, h->swi_lo, &h->swt_lo_n, h->sw_n2, h->sw_n1, N, +1, tab_fmt(h)));
+  } else {
+    TRY(make_twiddles(h->tw_r, h->nc, tab_fmt(h)));
+  }
   if (!h->kn.sw) TRY(make_twiddles(h->tw_c, h->nr, tab_fmt(h)));
   if (h->wn) TRY(make_twiddles(h->tw_w, h->wn, tab_fmt(h)));
 
@@ -927,7 +973,7 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
     for (int j = 0; j < M; ++j) ay[j] = -b_shy * cfg->dPP * (cfg->dX * ((double)j - 0.5 * M));
     TRY(make_shear(h->shx_hi, h->shx_lo, &h->shx_lo_n, ax, M, 1.0 / M, tab_fmt(h)));
     TRY(make_shear(h->shy_hi, h->shy_lo, &h->shy_lo_n, ay, M, 1.0 / M, tab_fmt(h)));
-  } else {
+  } else if (h->wn) {
     // schrodinger_wigner_cuda_1d.py:695-726: P is fft-shifted along the sheared axis
     const int M = h->wn;
     std::vector<double> ax(M), ay(M);
@@ -940,7 +986,7 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   if (h->kn.vn) TRY(make_twist(h->twist_hi, h->twist_lo, &h->twist_lo_n, h->nc, tab_fmt(h)));
 
   // reduction scratch of the Wigner column pass
-  const int wr = h->kn.rotated ? h->nr : h->wn, wc = h->kn.rotated ? h->nc : h->wn;
+  const int wr = h->kn.rotated ? h->nr : (h->wn ? h->wn : 32), wc = h->kn.rotated ? h->nc : (h->wn ? h->wn : 32);
   h->red_blocks = aw_col_pass_blocks(wr, wc, h->f32);
   if (h->ni > 1) {
     // a batch splits its columns the same way in every launch, chosen for the full batch
@@ -950,12 +996,14 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   }
   if (h->red_blocks <= 0) return fail(AW_E_ARG, "unsupported Wigner grid %d x %d", wr, wc);
   // per-instance reduction scratch (the pass kernels index it by instance)
-  TRY(dalloc(h->red_line, ni * (size_t)wc * 8));
-  TRY(dalloc(h->red_cross, ni * (size_t)h->red_blocks * wr * 8));
+  // (a wave function's marginals |psi|^2 and |fft psi|^2 also use red_line / red_cross)
+  TRY(dalloc(h->red_line, std::max(ni * (size_t)wc, h->kn.sw ? (size_t)N : 0) * 8));
+  TRY(dalloc(h->red_cross, std::max(ni * (size_t)h->red_blocks * wr, h->kn.sw ? (size_t)N : 0) * 8));
   TRY(dalloc(h->red_sq, ni * (size_t)h->red_blocks * 8));
-  TRY(dalloc(h->rowsum, (size_t)std::max(wr, wc) * 8));
+  TRY(dalloc(h->rowsum, std::max((size_t)std::max(wr, wc), h->kn.sw ? (size_t)N : 0) * 8));  // finalize: one per row
   TRY(dalloc(h->diag, ni * (size_t)std::max(h->nr, h->nc) * 16));
-  TRY(dalloc(h->abs2, 2 * ni * (size_t)std::max(h->nr, 1) * 8));  // two parities, see rot_run
+  // per-block norm partials: two parities (rot_run); a long wave function's column passes use up to N2
+  TRY(dalloc(h->abs2, 2 * ni * (size_t)std::max(std::max(h->nr, 1), h->sw_n2) * 8));
   if (h->kn.rotated) {
     // the marginal column pass: narrow slabs spread over every SM, row partials summed across
     // clusters of 8 blocks in distributed shared memory, so that z_blocks stays small
@@ -1003,7 +1051,8 @@ extern "C" int aw_create(const aw_config* cfg, aw_handle* out) {
 extern "C" int aw_destroy(aw_handle h) {
   if (!h) return AW_OK;
   if (h->st) cudaStreamSynchronize(h->st);
-  DevBuf* bufs[] = {&h->vseq, &h->vtimes, &h->zbuf, &h->altbuf, &h->twist_hi, &h->twist_lo, &h->rho, &h->W, &h->snap, &h->tmp, &h->stage, &h->tw_r, &h->tw_c, &h->tw_w, &h->shx_hi,
+  DevBuf* bufs[] = {&h->tw_l1, &h->tw_l2, &h->swf_hi, &h->swf_lo, &h->swi_hi, &h->swi_lo,
+                    &h->vseq, &h->vtimes, &h->zbuf, &h->altbuf, &h->twist_hi, &h->twist_lo, &h->rho, &h->W, &h->snap, &h->tmp, &h->stage, &h->tw_r, &h->tw_c, &h->tw_w, &h->shx_hi,
                     &h->shx_lo, &h->shy_hi, &h->shy_lo, &h->tabs, &h->maskx, &h->maskp, &h->red_line,
                     &h->red_cross, &h->red_sq, &h->rowsum, &h->diag, &h->abs2, &h->scal, &h->stop, &h->hist,
                     &h->terms, &h->part, &h->blk_tabs};
@@ -2289,12 +2338,96 @@ static AwPassArgs sw_args(aw_state_s* h) {
   return a;
 }
 
+// 1-D table of N entries (slot) as a factor of a wave-function pass; lin selects how a long wave
+// function's matrix view reads it (1: natural order, 2: the four-step spectrum order)
+static AwFactor sw_tab(aw_state_s* h, int slot, int lin) {
+  AwFactor f = ftab(h, slot);
+  f.row_tab = nullptr;
+  f.lin = h->sw_n1 ? lin : 0;
+  return f;
+}
+
+// pre (x) -> FFT -> mid (p) -> [IFFT -> post (x)] on a wave function, in -> out.
+//   Single tile (N <= 8192): one row pass.  Longer: psi as the N1 x N2 matrix n = n1 N2 + n2 and the
+//   four-step FFT (Bailey, "FFTs in external or hierarchical memory", 1990): column FFTs of length
+//   N1, the twiddle exp(-2 pi i n2 k1 / N), row FFTs of length N2; the spectrum sits in the order
+//   k = k1 + N1 k2 at (k1, k2), which the mid factor reads its table in (lin = 2), and the inverse
+//   retraces the steps.  fwd_only stops after mid; red_abs2 receives per-block sums of |out|^2.
+//   Returns the number of norm partials in *nparts.
+static int sw_run(aw_state_s* h, const void* in, void* out, const AwFactor& pre, const AwFactor& mid,
+                  const AwFactor& post, bool fwd_only, double* red_abs2, int* nparts) {
+  if (!h->sw_n1) {
+    AwPassArgs a = sw_args(h);
+    a.in = in;
+    a.out = out;
+    a.f0 = pre;
+    a.d1 = +1;
+    a.f1 = mid;
+    if (!fwd_only) {
+      a.d2 = -1;
+      a.f3 = post;
+    }
+    if (red_abs2) {
+      a.red_abs2 = red_abs2;
+      a.abs2_end = 1;
+    }
+    TRY(row_pass(h, a, h->tw_r));
+    if (nparts) *nparts = row_blocks(h, h->sw_rows, h->nc);
+    return AW_OK;
+  }
+  const int n1 = h->sw_n1, n2 = h->sw_n2;
+  auto twist = [&](bool inv) {
+    AwFactor f = fnone();
+    f.sh_hi = (inv ? h->swi_hi : h->swf_hi).p;
+    f.sh_lo = (inv ? h->swi_lo : h->swf_lo).p;
+    f.sh_lo_n = h->swt_lo_n;
+    f.active = 1;
+    return f;
+  };
+  AwPassArgs a = pnone(h);
+  a.nrows = n1;
+  a.ncols = n2;
+  a.in = in;
+  a.out = out;
+  a.f0 = pre;
+  a.d1 = +1;
+  a.f1 = twist(false);
+  TRY(col_pass(h, a, h->tw_l1));
+  a = pnone(h);
+  a.nrows = n1;
+  a.ncols = n2;
+  a.in = a.out = out;
+  a.d1 = +1;
+  a.f1 = mid;
+  if (!fwd_only) a.d2 = -1;
+  TRY(row_pass(h, a, h->tw_l2));
+  if (fwd_only) return AW_OK;
+  a = pnone(h);
+  a.nrows = n1;
+  a.ncols = n2;
+  a.in = a.out = out;
+  a.f0 = twist(true);
+  a.d1 = -1;
+  a.f1 = post;
+  if (red_abs2) {
+    a.red_abs2 = red_abs2;
+    a.abs2_end = 1;
+  }
+  TRY(col_pass(h, a, h->tw_l1));
+  if (nparts) *nparts = aw_col_pass_blocks(n1, n2, h->f32);
+  return AW_OK;
+}
+
 static int sw_finalize(aw_state_s* h, double t, double* hrow) {
   const int N = h->nc;
   double* xm = (double*)h->red_line.p;    // |psi_j|^2
   double* pmar = (double*)h->red_cross.p; // |(fft psi)_k|^2
   KL(aw_k_abs2(h->W.p, h->f32, N, xm, h->st));
-  KL(aw_k_abs2(h->tmp.p, h->f32, N, pmar, h->st));
+  if (h->sw_n1) {
+    KL(aw_k_abs2_perm(h->tmp.p, h->f32, N, h->sw_n1, pmar, h->st));
+  } else {
+    KL(aw_k_abs2(h->tmp.p, h->f32, N, pmar, h->st));
+  }
   FinalArgs f{xm, 1, N, pmar, 1, N, N / 2, nullptr, h->cfg.dX, dinv(h), 1, 1};
   return launch_finalize_args(h, f, t, hrow, 0);
 }
@@ -2309,38 +2442,20 @@ int sw_propagate(aw_state_s* h, long long steps, double* t) {
   const bool tdep = c.v_time_dependent || c.k_time_dependent || c.absx_mode == 2 || c.absp_mode == 2;
   KL(aw_k_set2(dinv(h), 1.0, 0.0, h->st));
   if (!tdep) TRY(sw_tables(h, times[1]));
-  const int nb = row_blocks(h, h->sw_rows, h->nc);
   for (long long n = 1; n <= steps; ++n) {
     if (tdep) TRY(sw_tables(h, times[n]));
-    AwPassArgs a = sw_args(h);
-    a.in = h->rho.p;
-    a.out = c.ehrenfest ? h->W.p : h->rho.p;
-    a.f0 = ftab(h, TAB_V1);
-    a.f0.row_tab = nullptr;
-    a.f0.scale_ptr = dinv(h);
-    a.d1 = +1;
-    a.f1 = ftab(h, TAB_K);
-    a.f1.row_tab = nullptr;
-    a.d2 = -1;
-    a.f3 = ftab(h, TAB_V1);
-    a.f3.row_tab = nullptr;
-    if (!c.ehrenfest) {
-      a.red_abs2 = (double*)h->abs2.p;
-      a.abs2_end = 1;
-    } else {
-      // psi' -> W buffer; its momentum representation -> tmp
-      a.br_out = nullptr;
-    }
-    TRY(row_pass(h, a, h->tw_r));
+    AwFactor pre = sw_tab(h, TAB_V1, 1);
+    pre.scale_ptr = dinv(h);
+    const AwFactor mid = sw_tab(h, TAB_K, 2), post = sw_tab(h, TAB_V1, 1);
+    int nb = 0;
     if (c.ehrenfest) {
-      AwPassArgs b = sw_args(h);
-      b.in = h->W.p;
-      b.out = h->tmp.p;
-      b.d1 = +1;
-      TRY(row_pass(h, b, h->tw_r));
+      // psi' -> W buffer; its momentum representation -> tmp
+      TRY(sw_run(h, h->rho.p, h->W.p, pre, mid, post, false, nullptr, nullptr));
+      TRY(sw_run(h, h->W.p, h->tmp.p, fnone(), fnone(), fnone(), true, nullptr, nullptr));
       TRY(sw_finalize(h, times[n], (double*)h->hist.p + (size_t)(n - 1) * h->hist_cols));
       CK(cudaMemcpyAsync(h->rho.p, h->W.p, (size_t)h->sw_rows * h->nc * h->esz, cudaMemcpyDeviceToDevice, h->st));
     } else {
+      TRY(sw_run(h, h->rho.p, h->rho.p, pre, mid, post, false, (double*)h->abs2.p, &nb));
       KL(aw_k_norm_finalize((const double*)h->abs2.p, nb, c.dX, dinv(h), nullptr, h->st));
     }
   }
@@ -2353,6 +2468,7 @@ int sw_propagate(aw_state_s* h, long long steps, double* t) {
 // get_wigner / get_wigner_blackman (schrodinger_wigner_cuda_1d.py:593-663)
 static int sw_get_wigner(aw_state_s* h, int blackman) {
   const int N = h->nc;
+  if (!h->wn) return fail(AW_E_STATE, "the Wigner function of a wave function longer than 8192 points (an N x N grid) is not formed");
   KL(aw_k_psi2rho(h->rho.p, h->f32, N, h->W.p, h->st));
   if (blackman) TRY(ensure_blackman(h, N, N));
   void* bcol = blackman ? h->blk_tabs.p : nullptr;
@@ -2404,24 +2520,11 @@ extern "C" int aw_sw_imag_steps(aw_handle h, int64_t steps, int32_t project) {
   // bloch_expV = exp(-dt/2 V(X, t_initial)), bloch_expK = exp(-dt K(P, t_initial))  (sw:834-854)
   TRY(build_tab(h, TAB_BV, 0, 1, c.t_initial, 0.0, -0.5 * c.dt, 0.0, 0.0, 0, 0.0));
   TRY(build_tab(h, TAB_BK, 1, 1, c.t_initial, 0.0, -c.dt, 0.0, 0.0, 0, 0.0));
-  const int nb = row_blocks(h, h->sw_rows, h->nc);
   const int N = h->nc;
   for (long long n = 0; n < steps; ++n) {
-    AwPassArgs a = sw_args(h);
-    a.in = a.out = h->rho.p;
-    a.f0 = ftab(h, TAB_BV);
-    a.f0.row_tab = nullptr;
-    a.d1 = +1;
-    a.f1 = ftab(h, TAB_BK);
-    a.f1.row_tab = nullptr;
-    a.d2 = -1;
-    a.f3 = ftab(h, TAB_BV);
-    a.f3.row_tab = nullptr;
-    if (!project) {
-      a.red_abs2 = (double*)h->abs2.p;
-      a.abs2_end = 1;
-    }
-    TRY(row_pass(h, a, h->tw_r));
+    int nb = 0;
+    TRY(sw_run(h, h->rho.p, h->rho.p, sw_tab(h, TAB_BV, 1), sw_tab(h, TAB_BK, 2), sw_tab(h, TAB_BV, 1), false,
+               project ? nullptr : (double*)h->abs2.p, &nb));
     if (!project) {
       // psi /= norm(psi) sqrt(dX)
       KL(aw_k_norm_finalize((const double*)h->abs2.p, nb, c.dX, dinv(h), nullptr, h->st));
@@ -2488,16 +2591,17 @@ extern "C" int aw_sw_energy(aw_handle h, double t, double* out) {
   double v, k, n1[2], n2[2];
   TRY(dsum(h, h->rho.p, h->nc, 2, 0, n1));
   TRY(aw_average(h, h->V.c_str(), t, &v));
-  AwPassArgs a = sw_args(h);
-  a.in = h->rho.p;
-  a.out = h->tmp.p;
-  a.d1 = +1;
-  TRY(row_pass(h, a, h->tw_r));
-  TRY(dsum(h, h->tmp.p, h->nc, 2, 0, n2));
-  // average of K over the momentum representation held in tmp
+  TRY(sw_run(h, h->rho.p, h->tmp.p, fnone(), fnone(), fnone(), true, nullptr, nullptr));
+  const void* src = h->tmp.p;
+  if (h->sw_n1) {
+    // the four-step spectrum into natural order (the W buffer is scratch for a long wave function)
+    KL(aw_k_unpermute(h->tmp.p, h->W.p, h->f32, h->nc, h->sw_n1, h->st));
+    src = h->W.p;
+  }
+  TRY(dsum(h, src, h->nc, 2, 0, n2));
+  // average of K over the momentum representation
   cudaKernel_t kern;
   TRY(get_obs_kernel(h, h->K.c_str(), &kern));
-  const void* src = h->tmp.p;
   int f32 = h->f32, nr = 1, nc = h->nc;
   double* part = (double*)h->part.p;
   double dX = h->cfg.dX, dP = h->cfg.dP;

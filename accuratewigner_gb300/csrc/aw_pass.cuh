@@ -48,7 +48,7 @@ __device__ __forceinline__ long long gidx(int lg, int pos, int ncols) {
 
 // apply one AwFactor to the thread's own elements
 template <typename V, class Tile, int NT>
-__device__ __forceinline__ void apply_factor(V* r, const AwFactor& f, int lg, int pos0, int ncols,
+__device__ __forceinline__ void apply_factor(V* r, const AwFactor& f, int lg, int pos0, int nrows, int ncols,
                                              long long tab_off, long long elem_off, int inst) {
   typedef typename RealOf<V>::type T;
   constexpr int E = Own<Tile, NT>::E;
@@ -64,7 +64,7 @@ __device__ __forceinline__ void apply_factor(V* r, const AwFactor& f, int lg, in
   // every factor that depends only on the line, folded into one complex constant:
   //   row tile: conj(row_tab[line]) * scale,  column tile: col_tab[line] * scale
   // (the FP64 scale is converted only when there is one: conversions run at the FP64 rate)
-  const V* lt = Tile::IS_ROW ? rt : ct;
+  const V* lt = f.lin ? nullptr : (Tile::IS_ROW ? rt : ct);
   const bool scaled = f.scale_ptr || f.scale != 1.0;
   V c;
   if (scaled) {
@@ -79,7 +79,7 @@ __device__ __forceinline__ void apply_factor(V* r, const AwFactor& f, int lg, in
     c = Tile::IS_ROW ? cconj_if(lt[lg], 0x80000000u) : lt[lg];
   }
   const bool have_c = lt || scaled;
-  const V* et = Tile::IS_ROW ? ct : rt;  // table along the line
+  const V* et = f.lin ? nullptr : (Tile::IS_ROW ? ct : rt);  // table along the line
   const int lo_n = f.sh_lo_n;
   const int nhi = lo_n ? Tile::N / lo_n : 0;
   const int sgn = f.sign;
@@ -96,6 +96,7 @@ __device__ __forceinline__ void apply_factor(V* r, const AwFactor& f, int lg, in
       v = cscale(v, q);
     }
     if (et) v = Tile::IS_ROW ? cmul_l(v, et[j]) : cmulc_l(v, et[i]);
+    if (f.lin) v = cmul_l(v, ct[f.lin == 1 ? (long long)i * ncols + j : i + (long long)nrows * j]);
     if (have_c) v = cmul_l(v, c);
     if (lo_n) {
       const int q = (pos + f.sh_roll) & (Tile::N - 1);
@@ -185,9 +186,9 @@ __global__ void __launch_bounds__(NT, (NT <= 128 ? 4 : (NT <= 256 ? 2 : 1))) aw_
     const AwFactor* pre = seg == 0 ? &a.f0 : (seg == 3 ? &a.f2 : nullptr);
     const AwFactor* post = seg == 0 ? &a.f1 : (seg == 1 ? &a.fbr : (seg == 3 ? &a.f3 : nullptr));
     const int dir = seg == 0 ? a.d1 : (seg == 1 ? a.br_d1 : (seg == 2 ? a.br_d2 : a.d2));
-    if (pre && pre->active) apply_factor<V, Tile, NT>(r, *pre, lg, pos0, ncols, toff, eoff, inst);
+    if (pre && pre->active) apply_factor<V, Tile, NT>(r, *pre, lg, pos0, a.nrows, ncols, toff, eoff, inst);
     run_fft<Tile, NT>(r, s, tw, dir, tid);
-    if (post && post->active) apply_factor<V, Tile, NT>(r, *post, lg, pos0, ncols, toff, eoff, inst);
+    if (post && post->active) apply_factor<V, Tile, NT>(r, *post, lg, pos0, a.nrows, ncols, toff, eoff, inst);
     if (seg == 0) {
       if (a.mid_out) store_regs<V, Tile, NT>((V*)a.mid_out + eoff, r, lg, pos0, ncols, a.mid_sign != 0);
       if (Tile::IS_ROW && a.diag_out) {
@@ -196,7 +197,7 @@ __global__ void __launch_bounds__(NT, (NT <= 128 ? 4 : (NT <= 256 ? 2 : 1))) aw_
           if (pos0 + k * STEP == lg)
             a.diag_out[(long long)inst * a.nrows + lg] = make_double2(to_d(r[k].x), to_d(r[k].y));
       }
-      if (Tile::IS_ROW && a.red_abs2 && !a.abs2_end) {
+      if (a.red_abs2 && !a.abs2_end) {
         T acc = from_double<T>(0.0);
 #pragma unroll
         for (int k = 0; k < E; ++k) acc += r[k].x * r[k].x + r[k].y * r[k].y;
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(NT, (NT <= 128 ? 4 : (NT <= 256 ? 2 : 1))) aw_
     }
   }
   if (a.out) store_regs<V, Tile, NT>((V*)a.out + eoff, r, lg, pos0, ncols, false);
-  if (Tile::IS_ROW && a.red_abs2 && a.abs2_end) {
+  if (a.red_abs2 && a.abs2_end) {
     T acc = from_double<T>(0.0);
 #pragma unroll
     for (int k = 0; k < E; ++k) acc += r[k].x * r[k].x + r[k].y * r[k].y;

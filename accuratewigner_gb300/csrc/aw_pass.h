@@ -32,6 +32,8 @@ typedef struct AwFactor {
   int sign;                 // 1: multiply by (-1)^(i+j); 2: by (-1)^i; 3: by (-1)^j
   int sh_lo_n;              // 0: no shear
   int sh_roll;              // shear position index is (pos + sh_roll) mod npos
+  int lin;                  // col_tab as one table over the grid read as a 1-D array: 1 at i * ncols + j
+                            // (row-major order), 2 at i + nrows * j (the four-step FFT's spectrum order)
   int active;
 } AwFactor;
 

@@ -187,11 +187,20 @@ __global__ void k_norm_finalize(const double* parts, int nparts, double scale, d
 }
 
 // |a|^2 as a real array
-__global__ void k_abs2(const void* a, int f32, long long n, double* out) {
+// |a_k|^2; with n1 > 0, a holds a spectrum in the four-step order (k = k1 + n1 k2 at k1 n2 + k2)
+__global__ void k_abs2(const void* a, int f32, long long n, double* out, int n1) {
+  const long long n2 = n1 > 0 ? n / n1 : 0;
   for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
-    double2 v = ld(a, k, f32);
+    double2 v = ld(a, n1 > 0 ? (k % n1) * n2 + k / n1 : k, f32);
     out[k] = v.x * v.x + v.y * v.y;
   }
+}
+
+// out[k] = a[(k % n1) n2 + k / n1]: a four-step spectrum into natural order
+__global__ void k_unpermute(const void* a, void* out, int f32, long long n, int n1) {
+  const long long n2 = n / n1;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    st(out, k, f32, ld(a, (k % n1) * n2 + k / n1, f32));
 }
 
 // partial sums of conj(a) * b (the reference's vdot ReductionKernel, sw:524-530)
@@ -304,7 +313,15 @@ int aw_k_norm_finalize(const double* parts, int nparts, double scale, double* in
   return ok();
 }
 int aw_k_abs2(const void* a, int f32, long long n, double* out, void* s) {
-  k_abs2<<<grid_for(n), 256, 0, (cudaStream_t)s>>>(a, f32, n, out);
+  k_abs2<<<grid_for(n), 256, 0, (cudaStream_t)s>>>(a, f32, n, out, 0);
+  return ok();
+}
+int aw_k_abs2_perm(const void* a, int f32, long long n, int n1, double* out, void* s) {
+  k_abs2<<<grid_for(n), 256, 0, (cudaStream_t)s>>>(a, f32, n, out, n1);
+  return ok();
+}
+int aw_k_unpermute(const void* a, void* out, int f32, long long n, int n1, void* s) {
+  k_unpermute<<<grid_for(n), 256, 0, (cudaStream_t)s>>>(a, out, f32, n, n1);
   return ok();
 }
 int aw_k_vdot(const void* a, const void* b, int f32, long long n, double2* part, int nblocks, void* s) {

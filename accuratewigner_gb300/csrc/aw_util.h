@@ -23,6 +23,10 @@ int aw_k_set2(double* p, double a, double b, void* s);
 int aw_k_sum_parts(const double2* part, int nparts, int n, double2* out, void* s);
 int aw_k_norm_finalize(const double* parts, int nparts, double scale, double* inv_out, double* hist, void* s);
 int aw_k_abs2(const void* a, int f32, long long n, double* out, void* s);
+// |a|^2 of a spectrum held in the four-step order (k = k1 + n1 k2 at k1 (n / n1) + k2), in natural order
+int aw_k_abs2_perm(const void* a, int f32, long long n, int n1, double* out, void* s);
+// a four-step spectrum into natural order
+int aw_k_unpermute(const void* a, void* out, int f32, long long n, int n1, void* s);
 int aw_k_vdot(const void* a, const void* b, int f32, long long n, double2* part, int nblocks, void* s);
 int aw_k_axpy(void* y, const void* x, int f32, long long n, double cr, double ci, void* s);
 

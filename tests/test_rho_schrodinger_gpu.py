@@ -135,3 +135,35 @@ def test_schrodinger_stationary_states():
     c.get_stationary_states(3, nsteps=300)
     for a, b in zip(g.stationary_states, c.stationary_states):
         assert rel_l2(a, b) < 1e-9
+
+
+@pytest.mark.parametrize("n", [16384, 32768])
+def test_schrodinger_long_wave_function_four_step(n):
+    """Wave functions longer than one pass tile (the reference's coherent_strong_field_physics_cuda_1d.py
+    uses X_gridDIM = 16 * 2048) go through the four-step transform."""
+    from accuratewigner_gb300 import SchrodingerWignerCUDA1D
+    from oracle.propagators import SchrodingerWignerOracle
+
+    p = dict(SW, X_gridDIM=n, X_amplitude=40.0)
+    g = SchrodingerWignerCUDA1D(**p)
+    c = SchrodingerWignerOracle(**p)
+    init = "exp(-pow(X - 1., 2) + cuda_complex(0., 0.5) * X)"
+    g.set_wavefunction(init)
+    c.set_wavefunction(init)
+    g.propagate(25)
+    c.propagate(25)
+    assert rel_l2(g.wavefunction.get(), c.wavefunction) < TOL
+    for name in ("X_average", "X_average_RHS", "P_average", "P_average_RHS", "hamiltonian_average"):
+        assert obs_close(getattr(g, name), getattr(c, name), TOL), name
+    q = {k: v for k, v in p.items() if k not in ("diff_K", "diff_V")}
+    g = SchrodingerWignerCUDA1D(**q)
+    c = SchrodingerWignerOracle(**q)
+    g.set_wavefunction("exp(-X * X)")
+    c.set_wavefunction("exp(-X * X)")
+    g.propagate(10)
+    c.propagate(10)
+    assert rel_l2(g.wavefunction.get(), c.wavefunction) < TOL
+    g.set_ground_state(200)
+    c.set_ground_state(200)
+    assert rel_l2(g.wavefunction.get(), c.wavefunction) < TOL
+    assert abs(g.get_energy() - c.get_energy()) < 1e-10
