@@ -287,6 +287,8 @@ class Engine:
     def run(self, requests, realtime=True):
         """Submit `requests` at their arrival times (seconds from now) and wait for all of them."""
         t0 = time.perf_counter()
+        with self.done_cv:
+            target = len(self.finished) + len(requests)  # an engine serves one stream after another
         for r in sorted(requests, key=lambda r: r.arrival):
             if realtime:
                 wait = t0 + r.arrival - time.perf_counter()
@@ -295,7 +297,7 @@ class Engine:
             r.arrival = time.perf_counter()
             self.submit(r)
         with self.done_cv:
-            while len(self.finished) < len(requests) and not self.errors:
+            while len(self.finished) < target and not self.errors:
                 self.done_cv.wait(timeout=1.0)
         if self.errors:
             raise self.errors[0]

@@ -19,6 +19,8 @@ Other workloads (one JSON line each, not the headline):
                             double well and temperature; purity and energy against complex128
   --workload served         Poisson stream of Wigner-Moyal / von Neumann / rho-Bloch requests through
                             the continuous-batching loop: p50 / p99 latency and aggregate throughput
+  --workload served-sweep   the served stream at several arrival rates (--rates): achieved vs offered
+                            load, p50 / p99 per rate and the knee rate
   --workload large-vn       von Neumann 4096 x 4096, driven Morse potential, 2000 steps
   --workload precision      the headline workload in complex128 (double-float), complex64 and native
                             FP64 side by side: errors of W and of <x>, <p>, dipole acceleration per step
@@ -513,6 +515,39 @@ def run_served(args):
            "mean_latency_s": float(lat.mean()), "p50_latency_by_kind_s": by_kind, "clocks": clk.summary()})
 
 
+def run_served_sweep(args):
+    """The served stream at several Poisson rates (one warmed engine, the same seeded requests at each
+    rate, arrival times scaled by 1/rate): achieved against offered grid-pt*steps/s and p50/p99
+    latency per rate.  The knee is the highest rate at which the loop still delivers >= 90 % of the
+    offered load."""
+    from accuratewigner_gb300.serve import Engine, make_stream
+
+    rates = [float(r) for r in args.rates.split(",")]
+    eng = Engine(precision=args.precision, chunk=200)
+    eng.warm()
+    sweep = []
+    with ClockSampler(0) as clk:
+        for rate in rates:
+            reqs = make_stream(args.requests, rate, seed=0)
+            span = max(r.arrival for r in reqs)
+            work = float(sum(r.work for r in reqs))
+            wall = eng.run(reqs)
+            lat = np.array([r.latency for r in reqs])
+            sweep.append({"rate_per_s": rate, "offered": work / span, "achieved": work / wall, "wall_s": wall,
+                          "p50_latency_s": float(np.percentile(lat, 50)),
+                          "p99_latency_s": float(np.percentile(lat, 99))})
+    eng.close()
+    keeps_up = [s["rate_per_s"] for s in sweep if s["achieved"] >= 0.9 * s["offered"]]
+    best = max(s["achieved"] for s in sweep)
+    _line("served-sweep", "grid-pt*steps/s (aggregate, best over the rate sweep) with the knee rate", best,
+          "grid-pt*steps/s", sum(s["wall_s"] for s in sweep), args,
+          {"requests_per_rate": args.requests, "rates_per_s": rates, "seed": 0, "sides": [128, 256, 512, 1024, 2048],
+           "steps": "U(100, 5000)", "kinds": ["wigner-moyal (Ehrenfest)", "von Neumann", "rho-Bloch Gibbs"],
+           "chunk_steps": 200, "precision": args.precision,
+           "knee": "highest rate whose achieved throughput is >= 90 % of the offered load"},
+          {"knee_rate_per_s": max(keeps_up) if keeps_up else None, "sweep": sweep, "clocks": clk.summary()})
+
+
 def run_large_vn(args):
     """von Neumann 4096 x 4096, X_amplitude = 80, Morse V = D (1 - exp(-alpha (x - x0)))^2 + x 0.02 sin(0.01 t)
     (D = 0.18, alpha = 1, x0 = 1.4), dt = 0.02, 2000 steps; rho0 = sum of 8 seeded Gaussian pure states."""
@@ -568,15 +603,17 @@ def main():
     ap.add_argument("--precision", default="c128", choices=["c128", "c128-fp64", "c64", "auto"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="strong-field",
-                    choices=["strong-field", "plain", "batched-gibbs", "served", "large-vn", "precision"])
-    ap.add_argument("--requests", type=int, default=60, help="served: number of requests")
+                    choices=["strong-field", "plain", "batched-gibbs", "served", "served-sweep", "large-vn",
+                             "precision"])
+    ap.add_argument("--requests", type=int, default=60, help="served: number of requests (per rate for the sweep)")
     ap.add_argument("--rate", type=float, default=4.0, help="served: Poisson arrival rate per second")
+    ap.add_argument("--rates", default="1,1.5,2,3,4", help="served-sweep: comma-separated arrival rates per second")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    other = {"plain": run_plain, "batched-gibbs": run_batched_gibbs, "served": run_served, "large-vn": run_large_vn,
-             "precision": run_precision}
-    if args.precision == "auto" and args.workload != "served":
+    other = {"plain": run_plain, "batched-gibbs": run_batched_gibbs, "served": run_served,
+             "served-sweep": run_served_sweep, "large-vn": run_large_vn, "precision": run_precision}
+    if args.precision == "auto" and args.workload not in ("served", "served-sweep"):
         ap.error("--precision auto chooses per request: only the served workload has requests")
     if args.workload in other:
         import torch
