@@ -24,6 +24,8 @@ Other workloads (one JSON line each, not the headline):
   --workload large-vn       von Neumann 4096 x 4096, driven Morse potential, 2000 steps
   --workload precision      the headline workload in complex128 (double-float), complex64 and native
                             FP64 side by side: errors of W and of <x>, <p>, dipole acceleration per step
+  --workload frames         the headline workload writing a frame (W, t, diagonal of rho) every 100
+                            steps through the asynchronous run record, against no frames
 """
 import argparse
 import ctypes
@@ -548,6 +550,49 @@ def run_served_sweep(args):
           {"knee_rate_per_s": max(keeps_up) if keeps_up else None, "sweep": sweep, "clocks": clk.summary()})
 
 
+def run_frames(args):
+    """The headline run with its on-disk record: a frame (W, t, diagonal of rho) saved every 100 steps
+    through the asynchronous writer, against the same steps without frames."""
+    import shutil
+    import tempfile
+
+    import torch
+
+    from accuratewigner_gb300.records import RunRecord
+
+    prop = make_propagator(args.precision)
+    chunk, frames = 100, 10
+    prop.propagate(chunk)  # warm-up
+
+    def plain():
+        for _ in range(frames):
+            prop.propagate(chunk)
+        torch.cuda.synchronize()
+
+    d = tempfile.mkdtemp(prefix="aw_frames_")
+
+    def recorded():
+        with RunRecord(d, prop, PARAMS) as rec:
+            for _ in range(frames):
+                prop.propagate(chunk)
+                rec.save_frame()
+
+    try:
+        with ClockSampler(0) as clk:
+            t_plain, _ = _timed(plain)
+            t_rec, _ = _timed(recorded)
+        frame_bytes = os.path.getsize(os.path.join(d, "frames", "0.npz"))
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    work = float(N_GRID * N_GRID * chunk * frames)
+    _line("frames", "grid-pt*steps/s with a frame written every 100 steps", work / t_rec, "grid-pt*steps/s", t_rec,
+          args, {"workload": "strong-field Wigner-Moyal 1024x1024 (the headline)", "steps": chunk * frames,
+                 "frame_every_steps": chunk, "frame": "W real part, t, diagonal of rho (.npz)",
+                 "precision": args.precision},
+          {"without_frames": work / t_plain, "overhead_fraction": t_rec / t_plain - 1.0,
+           "bytes_per_frame": frame_bytes, "clocks": clk.summary()})
+
+
 def run_large_vn(args):
     """von Neumann 4096 x 4096, X_amplitude = 80, Morse V = D (1 - exp(-alpha (x - x0)))^2 + x 0.02 sin(0.01 t)
     (D = 0.18, alpha = 1, x0 = 1.4), dt = 0.02, 2000 steps; rho0 = sum of 8 seeded Gaussian pure states."""
@@ -604,7 +649,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="strong-field",
                     choices=["strong-field", "plain", "batched-gibbs", "served", "served-sweep", "large-vn",
-                             "precision"])
+                             "precision", "frames"])
     ap.add_argument("--requests", type=int, default=60, help="served: number of requests (per rate for the sweep)")
     ap.add_argument("--rate", type=float, default=4.0, help="served: Poisson arrival rate per second")
     ap.add_argument("--rates", default="1,1.5,2,3,4", help="served-sweep: comma-separated arrival rates per second")
@@ -612,7 +657,8 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     other = {"plain": run_plain, "batched-gibbs": run_batched_gibbs, "served": run_served,
-             "served-sweep": run_served_sweep, "large-vn": run_large_vn, "precision": run_precision}
+             "served-sweep": run_served_sweep, "large-vn": run_large_vn, "precision": run_precision,
+             "frames": run_frames}
     if args.precision == "auto" and args.workload not in ("served", "served-sweep"):
         ap.error("--precision auto chooses per request: only the served workload has requests")
     if args.workload in other:
