@@ -35,7 +35,9 @@ def test_ground_state_is_the_lowest_band_and_stays_put():
     r = s.rho.get()
     r = r / np.trace(r)
     q = lattice(256)
-    assert np.linalg.norm(r - q.get_gibbs(0.0, 0.5, n=1)) < 1e-8
+    # splitting error of the imaginary-time step that the dbeta halvings ended on (3e-9 in the FP64
+    # oracle, 2e-8 with double-float passes, whose purity test stops at another step)
+    assert np.linalg.norm(r - q.get_gibbs(0.0, 0.5, n=1)) < 1e-7
     assert abs(q.get_energy(r) - mathieu_levels(False, 1)[0]) < 1e-8
     # a stationary state: real-time propagation leaves it in place (bsg:190-192), up to the
     # splitting error of the real-time step (the exact band state drifts by 1.8e-6 over these 200
