@@ -337,10 +337,11 @@ static double define_round(double v) {
 }
 
 // Element format of the tables the passes read: 0 FP64, 1 FP32, 2 double-float
-// (each FP64 number as the FP32 pair hi = rn(v), lo = rn(v - hi)).
+// (each FP64 number as the FP32 pair hi = rn(v), lo = rn(v - hi); a complex entry as
+// (re hi, im hi, re lo, im lo)).
 static int tab_fmt(const aw_state_s* h) { return h->f32 ? 1 : (h->df ? 2 : 0); }
 
-// upload real numbers (interleaved re, im for complex tables) in table format fmt
+// upload a complex table (interleaved re, im) in table format fmt
 static int upload_reals(DevBuf& dst, const std::vector<double>& v, int fmt) {
   const size_t n = v.size();
   TRY(dalloc(dst, n * (fmt == 1 ? 4 : 8)));
@@ -351,11 +352,14 @@ static int upload_reals(DevBuf& dst, const std::vector<double>& v, int fmt) {
     std::vector<float> g(v.begin(), v.end());
     CK(cudaMemcpy(dst.p, g.data(), n * 4, cudaMemcpyHostToDevice));
   } else {
+    // complex entries (re, im) as (re hi, im hi, re lo, im lo)
     std::vector<float> g(2 * n);
-    for (size_t k = 0; k < n; ++k) {
-      const float hi = (float)v[k];
-      g[2 * k] = hi;
-      g[2 * k + 1] = (float)(v[k] - (double)hi);
+    for (size_t k = 0; k + 1 < n; k += 2) {
+      const float rh = (float)v[k], ih = (float)v[k + 1];
+      g[2 * k] = rh;
+      g[2 * k + 1] = ih;
+      g[2 * k + 2] = (float)(v[k] - (double)rh);
+      g[2 * k + 3] = (float)(v[k + 1] - (double)ih);
     }
     CK(cudaMemcpy(dst.p, g.data(), n * 8, cudaMemcpyHostToDevice));
   }

@@ -3,8 +3,9 @@
 // The reference keeps every state in pycuda::complex<double>
 // (wigner_moyal_cuda_1d.py:629); here a state element is a CUDA vector type:
 // double2 for the native complex128 form, float2 for the complex64 form and
-// dfc (a double-float complex of four FP32 numbers, also 16 bytes) for the
-// complex128 form computed on the FP32 pipes.
+// dfc (a double-float complex of two packed FP32 pairs, also 16 bytes) for the
+// complex128 form computed on the FP32 pipes.  Element-wise code reads the
+// parts through cre / cim and builds elements with cmake.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -69,8 +70,8 @@ template <typename V> struct cpart {
 };
 template <> struct cpart<dfc> {
   typedef dfc type;
-  __device__ static dfc make(dfr x, dfr y) { return dfc{x, y}; }
-  __device__ static dfc zero() { return dfc{dfr{0.f, 0.f}, dfr{0.f, 0.f}}; }
+  __device__ static dfc make(dfr x, dfr y) { return dfc_make(x, y); }
+  __device__ static dfc zero() { return dfc{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}; }
   __device__ static dfc add(dfc a, dfc b) { return dfc_add(a, b); }
   __device__ static double2 to_d2(dfc a) { return dfc_to_double2(a); }
 };
@@ -82,6 +83,19 @@ __device__ __forceinline__ V cmake(typename scalar_of<V>::type x, typename scala
   r.y = y;
   return r;
 }
+template <> __device__ __forceinline__ dfc cmake<dfc>(dfr x, dfr y) { return dfc_make(x, y); }
+
+// real and imaginary parts
+template <typename V> __device__ __forceinline__ typename scalar_of<V>::type cre(V a) { return a.x; }
+template <typename V> __device__ __forceinline__ typename scalar_of<V>::type cim(V a) { return a.y; }
+template <> __device__ __forceinline__ dfr cre<dfc>(dfc a) { return dfc_re(a); }
+template <> __device__ __forceinline__ dfr cim<dfc>(dfc a) { return dfc_im(a); }
+
+// |a|^2 in the working precision
+template <typename V> __device__ __forceinline__ typename scalar_of<V>::type cabs2(V a) {
+  return a.x * a.x + a.y * a.y;
+}
+template <> __device__ __forceinline__ dfr cabs2<dfc>(dfc a) { return dfc_abs2(a); }
 
 template <typename V> __device__ __forceinline__ V cadd(V a, V b) { return cmake<V>(a.x + b.x, a.y + b.y); }
 template <typename V> __device__ __forceinline__ V csub(V a, V b) { return cmake<V>(a.x - b.x, a.y - b.y); }
@@ -112,8 +126,11 @@ __device__ __forceinline__ double flip(double v, unsigned m) {
   return __hiloint2double(__double2hiint(v) ^ (int)m, __double2loint(v));
 }
 __device__ __forceinline__ dfr flip(dfr v, unsigned m) { return dfr{flip(v.h, m), flip(v.l, m)}; }
+__device__ __forceinline__ float2 flip(float2 v, unsigned mx, unsigned my) { return make_float2(flip(v.x, mx), flip(v.y, my)); }
 template <typename V> __device__ __forceinline__ V cflip(V a, unsigned m) { return cmake<V>(flip(a.x, m), flip(a.y, m)); }
 template <typename V> __device__ __forceinline__ V cconj_if(V a, unsigned m) { return cmake<V>(a.x, flip(a.y, m)); }
+template <> __device__ __forceinline__ dfc cflip<dfc>(dfc a, unsigned m) { return dfc{flip(a.h, m, m), flip(a.l, m, m)}; }
+template <> __device__ __forceinline__ dfc cconj_if<dfc>(dfc a, unsigned m) { return dfc{flip(a.h, 0u, m), flip(a.l, 0u, m)}; }
 
 // butterfly sums: for dfc without renormalisation (cnorm renormalises once at a butterfly's end);
 // the same as cadd / csub for the native types
@@ -136,6 +153,10 @@ template <> __device__ __forceinline__ dfc cmulc_l<dfc>(dfc a, dfc b) { return d
 template <typename V> __device__ __forceinline__ V cmul_mi_dir(V a, unsigned inv) {
   return cmake<V>(flip(a.y, inv), flip(a.x, inv ^ 0x80000000u));
 }
+template <> __device__ __forceinline__ dfc cmul_mi_dir<dfc>(dfc a, unsigned inv) {
+  const unsigned m = inv ^ 0x80000000u;
+  return dfc{flip(p_swap(a.h), inv, m), flip(p_swap(a.l), inv, m)};
+}
 
 // 1/sqrt(2) in the working type (double-float: the FP32 pair nearest to it)
 template <typename T> __device__ __forceinline__ T rsqrt2() { return T(0.70710678118654752440); }
@@ -146,6 +167,13 @@ template <typename V> __device__ __forceinline__ V cmul_w8_1_dir(V a, unsigned i
   typedef typename scalar_of<V>::type T;
   const T h = rsqrt2<T>();
   return cmake<V>((a.x + flip(a.y, inv)) * h, (a.y - flip(a.x, inv)) * h);
+}
+// double-float: a + (y, -x) forward, a + (-y, x) inverse on both lanes, then the scale, one
+// renormalisation at the end
+template <> __device__ __forceinline__ dfc cmul_w8_1_dir<dfc>(dfc a, unsigned inv) {
+  const unsigned m = inv ^ 0x80000000u;
+  const dfc t = dfc{flip(p_swap(a.h), inv, m), flip(p_swap(a.l), inv, m)};  // a * (-+ i)
+  return dfc_renorm(dfc_scale_lazy(dfc_renorm(dfc_add_lazy(a, t)), rsqrt2<dfr>()));
 }
 // a * exp(-+ 3 i pi/4) = (a * exp(-+ i pi/4)) * (-+ i)
 template <typename V> __device__ __forceinline__ V cmul_w8_3_dir(V a, unsigned inv) {

@@ -71,14 +71,15 @@ template <> __device__ inline void aw_store<double>(void* aw_p, long long aw_k, 
 template <> __device__ inline void aw_store<cuda_complex>(void* aw_p, long long aw_k, int aw_f32, cuda_complex aw_v) {
   if (aw_f32) ((float2*)aw_p)[aw_k] = make_float2((float)aw_v._aw_re, (float)aw_v._aw_im);
   else ((double2*)aw_p)[aw_k] = make_double2(aw_v._aw_re, aw_v._aw_im); }
-// double-float form of a table entry (format 2): each FP64 number as the FP32 pair (hi, lo)
+// double-float form of a table entry (format 2): each FP64 number as the FP32 pair (hi, lo); a
+// complex entry as (re hi, im hi, re lo, im lo)
 __device__ inline float2 aw_df1(double aw_v) {
   const float aw_h = (float)aw_v;
   return make_float2(aw_h, (float)(aw_v - (double)aw_h));
 }
 __device__ inline float4 aw_df2(double aw_re, double aw_im) {
   const float2 aw_a = aw_df1(aw_re), aw_b = aw_df1(aw_im);
-  return make_float4(aw_a.x, aw_a.y, aw_b.x, aw_b.y);
+  return make_float4(aw_a.x, aw_b.x, aw_a.y, aw_b.y);
 }
 __device__ inline double2 aw_load(const void* aw_p, long long aw_k, int aw_f32) {
   if (aw_f32) { float2 aw_v = ((const float2*)aw_p)[aw_k]; return make_double2(aw_v.x, aw_v.y); }

@@ -195,12 +195,12 @@ __global__ void __launch_bounds__(NT, (NT <= 128 ? 4 : (NT <= 256 ? 2 : 1))) aw_
 #pragma unroll
         for (int k = 0; k < E; ++k)
           if (pos0 + k * STEP == lg)
-            a.diag_out[(long long)inst * a.nrows + lg] = make_double2(to_d(r[k].x), to_d(r[k].y));
+            a.diag_out[(long long)inst * a.nrows + lg] = make_double2(to_d(cre(r[k])), to_d(cim(r[k])));
       }
       if (a.red_abs2 && !a.abs2_end) {
         T acc = from_double<T>(0.0);
 #pragma unroll
-        for (int k = 0; k < E; ++k) acc += r[k].x * r[k].x + r[k].y * r[k].y;
+        for (int k = 0; k < E; ++k) acc += cabs2(r[k]);
         const double tot = block_sum<NT>(to_d(acc), red, tid);
         if (tid == 0) a.red_abs2[(long long)inst * gridDim.x + blockIdx.x] = tot;
       }
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(NT, (NT <= 128 ? 4 : (NT <= 256 ? 2 : 1))) aw_
   if (a.red_abs2 && a.abs2_end) {
     T acc = from_double<T>(0.0);
 #pragma unroll
-    for (int k = 0; k < E; ++k) acc += r[k].x * r[k].x + r[k].y * r[k].y;
+    for (int k = 0; k < E; ++k) acc += cabs2(r[k]);
     const double tot = block_sum<NT>(to_d(acc), red, tid);
     if (tid == 0) a.red_abs2[(long long)inst * gridDim.x + blockIdx.x] = tot;
   }
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(NT, (NT <= 128 ? 4 : (NT <= 256 ? 2 : 1))) aw_
 #pragma unroll
       for (int k = 0; k < E; ++k) {
         const int pos = pos0 + k * STEP;
-        const T re = r[k].x, im = r[k].y;
+        const T re = cre(r[k]), im = cim(r[k]);
         if (pos & 1) {
           cr -= re;
           ci -= im;
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(NT, (NT <= 128 ? 4 : (NT <= 256 ? 2 : 1))) aw_
 #pragma unroll
       for (int k = 0; k < E; ++k) {
         const int pos = pos0 + k * STEP;
-        const A re = to_acc<A>(r[k].x), im = to_acc<A>(r[k].y);
+        const A re = to_acc<A>(cre(r[k])), im = to_acc<A>(cim(r[k]));
         lsum += re;
         sq += re * re - im * im;
         if (a.red_cross) {

@@ -10,7 +10,7 @@
 
 namespace {
 
-// element formats: 0 complex128, 1 complex64, 2 double-float complex (re hi, re lo, im hi, im lo)
+// element formats: 0 complex128, 1 complex64, 2 double-float complex (re hi, im hi, re lo, im lo)
 __device__ __forceinline__ double2 ld(const void* p, long long k, int f32) {
   if (f32 == 1) {
     float2 v = ((const float2*)p)[k];
@@ -18,7 +18,7 @@ __device__ __forceinline__ double2 ld(const void* p, long long k, int f32) {
   }
   if (f32 == 2) {
     float4 v = ((const float4*)p)[k];
-    return make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+    return make_double2((double)v.x + (double)v.z, (double)v.y + (double)v.w);
   }
   return ((const double2*)p)[k];
 }
@@ -31,7 +31,7 @@ __device__ __forceinline__ void st(void* p, long long k, int f32, double2 v) {
     ((float2*)p)[k] = make_float2((float)v.x, (float)v.y);
   } else if (f32 == 2) {
     const float2 a = df_split(v.x), b = df_split(v.y);
-    ((float4*)p)[k] = make_float4(a.x, a.y, b.x, b.y);
+    ((float4*)p)[k] = make_float4(a.x, b.x, a.y, b.y);
   } else {
     ((double2*)p)[k] = v;
   }
