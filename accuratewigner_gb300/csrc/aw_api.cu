@@ -212,18 +212,18 @@ struct aw_state_s {
 // launch classes of the profiler
 enum { PROF_ROW = 0, PROF_COL = 1, PROF_JIT = 2, PROF_UTIL = 3, PROF_NCLS = 4 };
 
-static cudaEvent_t prof_mark(aw_state_s* h) {
+static cudaEvent_t prof_mark(aw_state_s* h, cudaStream_t st = nullptr) {
   cudaEvent_t e = nullptr;
   if (!h->prof_on) return e;
   cudaEventCreate(&e);
-  cudaEventRecord(e, h->st);
+  cudaEventRecord(e, st ? st : h->st);
   return e;
 }
-static void prof_done(aw_state_s* h, int cls, double bytes, cudaEvent_t a) {
+static void prof_done(aw_state_s* h, int cls, double bytes, cudaEvent_t a, cudaStream_t st = nullptr) {
   if (!h->prof_on || !a) return;
   cudaEvent_t b;
   cudaEventCreate(&b);
-  cudaEventRecord(b, h->st);
+  cudaEventRecord(b, st ? st : h->st);
   h->prof.push_back({cls, bytes, a, b});
 }
 static void prof_clear(aw_state_s* h) {
@@ -540,13 +540,13 @@ struct Settled {
 static void* df_region(const AwPassArgs& a, const void* base) {
   return base ? (char*)base + (size_t)a.inst0 * a.batch_elems * 16 : nullptr;
 }
-static int df_prepare(aw_state_s* h, AwPassArgs& a, int batch) {
+static int df_prepare(aw_state_s* h, AwPassArgs& a, int batch, cudaStream_t st) {
   const long long n = (long long)batch * a.batch_elems;
   void* rin = df_region(a, a.in);
   if (rin && !df_is_live(h, rin)) {
     void* base = a.out ? a.out : (void*)a.in;
     void* dst = df_region(a, base);
-    KL(aw_k_convert(rin, 0, dst, 2, n, h->st));
+    KL(aw_k_convert(rin, 0, dst, 2, n, st));
     a.in = base;
     df_mark(h, dst, n);
   }
@@ -559,7 +559,9 @@ static void df_outputs(aw_state_s* h, const AwPassArgs& a, int batch) {
   df_mark(h, df_region(a, a.br_out), n);
 }
 
-static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row) {
+// `st`: the stream of the launch (the handle's own when null)
+static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row, cudaStream_t st = nullptr) {
+  if (!st) st = h->st;
   a.tw = tw.p;
   const int batch = h->vc;
   if (h->ni > 1) {
@@ -569,16 +571,16 @@ static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row)
     if (!row && !a.lines_hint) a.lines_hint = h->col_lines;
   }
   if (row && !a.row_lines) a.row_lines = row_lines(h, a.nrows, a.ncols);
-  if (h->df) TRY(df_prepare(h, a, batch));
-  cudaEvent_t pe = prof_mark(h);
+  if (h->df) TRY(df_prepare(h, a, batch, st));
+  cudaEvent_t pe = prof_mark(h, st);
   int r;
   if (h->df)
-    r = row ? aw_launch_row_pass_df(&a, batch, h->st) : aw_launch_col_pass_df(&a, batch, h->st);
+    r = row ? aw_launch_row_pass_df(&a, batch, st) : aw_launch_col_pass_df(&a, batch, st);
   else if (h->f32)
-    r = row ? aw_launch_row_pass_f32(&a, batch, h->st) : aw_launch_col_pass_f32(&a, batch, h->st);
+    r = row ? aw_launch_row_pass_f32(&a, batch, st) : aw_launch_col_pass_f32(&a, batch, st);
   else
-    r = row ? aw_launch_row_pass_f64(&a, batch, h->st) : aw_launch_col_pass_f64(&a, batch, h->st);
-  prof_done(h, row ? PROF_ROW : PROF_COL, pass_bytes(h, a) * batch, pe);
+    r = row ? aw_launch_row_pass_f64(&a, batch, st) : aw_launch_col_pass_f64(&a, batch, st);
+  prof_done(h, row ? PROF_ROW : PROF_COL, pass_bytes(h, a) * batch, pe, st);
   ++g_launches;
   if (r)
     return fail(AW_E_CUDA, "%s pass launch failed (%d, %s), grid %d x %d", row ? "row" : "column", r,
@@ -587,7 +589,9 @@ static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row)
   return AW_OK;
 }
 static int row_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw) { return launch_pass(h, a, tw, true); }
-static int col_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw) { return launch_pass(h, a, tw, false); }
+static int col_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, cudaStream_t st = nullptr) {
+  return launch_pass(h, a, tw, false, st);
+}
 
 static void* tab_col(aw_state_s* h, int slot) { return (char*)h->tabs.p + (size_t)slot * (h->nc + h->nr) * h->esz; }
 static void* tab_row(aw_state_s* h, int slot) { return (char*)tab_col(h, slot) + (size_t)h->nc * h->esz; }
@@ -1661,6 +1665,11 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
   // normalize_rho_wigner (wm:608-622) is deferred to the end of the call: the step loop does not
   // wait for the reduction, which runs on a side stream.  Bloch steps normalise every step.
   const bool defer = !p.bloch && p.ehrenfest && h->st2;
+  // With the deferred reduction the marginal pass of step n runs on the side stream as well, where
+  // it overlaps the column and row passes of step n + 1 (and fills their last partial waves of
+  // blocks).  The branch outputs then alternate between W and tmp, the last step's in W, so that a
+  // row pass never overwrites a branch output that a marginal pass may still read.
+  auto wbuf = [&](long long n) -> void* { return (!defer || ((steps - n) & 1) == 0) ? h->W.p : h->tmp.p; };
   // scale applied in the column pass: 1/N^2 and, for Bloch steps, 1/norm of the previous step
   TRY(vinv_reset(h));
   TRY(reset_stops(h));  // a stop raised by an earlier call must not persist
@@ -1708,8 +1717,6 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
   for (long long n = 1; n <= steps; ++n) {
     const bool last = n == steps;
     const int par = defer ? (int)(n & 1) : 0;
-    // the reduction of step n - 2 read this parity's buffers
-    if (defer && n >= 3) CK(cudaStreamWaitEvent(h->st, h->ev_f[par], 0));
     // column pass: scale, ifft0, K-kick, fft0
     {
       if (kdep) TRY(rot_tables_K(h, p, times[n]));
@@ -1734,6 +1741,8 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       a.lines_hint = h->tuned_col_lines;
       TRY(col_pass(h, a, h->tw_c));
     }
+    // the marginal pass and reduction of step n - 2 read this parity's branch output and sums
+    if (defer && n >= 3) CK(cudaStreamWaitEvent(h->st, h->ev_f[par], 0));
     // row pass: ifft1, V-kick(t_n) [branch: Wigner transform] [next kick(t_{n+1}), fft1 | S]
     {
       AwPassArgs a = pnone(h);
@@ -1741,7 +1750,7 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       a.d1 = -1;
       TRY(vfactor(n, false, &a.f1));
       if (p.ehrenfest) {
-        a.br_out = h->W.p;
+        a.br_out = wbuf(n);
         a.br_d1 = +1;
         a.fbr = fshear_x(h);
         a.br_d2 = -1;
@@ -1766,7 +1775,7 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       // by alternating sums (aw_finalize_rot), so this column pass runs one FFT per column and writes
       // nothing back.  The last step completes W.
       AwPassArgs a = pnone(h);
-      a.in = h->W.p;
+      a.in = wbuf(n);
       a.d1 = +1;
       a.f1 = fshear_y(h);
       a.col_alt = zbuf_of(h, par);
@@ -1774,17 +1783,21 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       a.lines_hint = h->z_lines;
       a.cluster = h->z_cluster;
       a.stop = stop;
-      TRY(col_pass(h, a, h->tw_c));
       double* hrow = hist + (size_t)(n - 1) * h->hist_cols;
       if (defer) {
+        // after the row pass of step n, on the side stream: marginal pass, then the reduction
         CK(cudaEventRecord(h->ev_z[par], h->st));
         CK(cudaStreamWaitEvent(h->st2, h->ev_z[par], 0));
+        TRY(col_pass(h, a, h->tw_c, h->st2));
         TRY(launch_finalize_rot(h, times[n], hrow, 0, par, h->st2));
         CK(cudaEventRecord(h->ev_f[par], h->st2));
       } else {
+        TRY(col_pass(h, a, h->tw_c));
         TRY(launch_finalize_rot(h, times[n], hrow, p.stop_on_purity));
       }
       if (last) {
+        // completes W in place: after the marginal pass has read it
+        if (defer) CK(cudaStreamWaitEvent(h->st, h->ev_f[par], 0));
         WignerGrid g{h->W.p, h->nr, h->nc, &h->tw_r, &h->tw_c};
         TRY(wigner_passes(h, g, h->W.p, fnone(), false, false, true, true));
       }

@@ -168,12 +168,13 @@ template <typename V> __device__ __forceinline__ V cmul_w8_1_dir(V a, unsigned i
   const T h = rsqrt2<T>();
   return cmake<V>((a.x + flip(a.y, inv)) * h, (a.y - flip(a.x, inv)) * h);
 }
-// double-float: a + (y, -x) forward, a + (-y, x) inverse on both lanes, then the scale, one
-// renormalisation at the end
+// double-float: a + (y, -x) forward, a + (-y, x) inverse on both lanes, then the scale; the lazy
+// sum feeds the product directly (its low part enters through the cross term) and one
+// renormalisation ends it
 template <> __device__ __forceinline__ dfc cmul_w8_1_dir<dfc>(dfc a, unsigned inv) {
   const unsigned m = inv ^ 0x80000000u;
   const dfc t = dfc{flip(p_swap(a.h), inv, m), flip(p_swap(a.l), inv, m)};  // a * (-+ i)
-  return dfc_renorm(dfc_scale_lazy(dfc_renorm(dfc_add_lazy(a, t)), rsqrt2<dfr>()));
+  return dfc_renorm(dfc_scale_lazy(dfc_add_lazy(a, t), rsqrt2<dfr>()));
 }
 // a * exp(-+ 3 i pi/4) = (a * exp(-+ i pi/4)) * (-+ i)
 template <typename V> __device__ __forceinline__ V cmul_w8_3_dir(V a, unsigned inv) {
