@@ -1014,10 +1014,10 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   TRY(dalloc(h->abs2, 2 * ni * (size_t)std::max(std::max(h->nr, 1), h->sw_n2) * 8));
   if (h->kn.rotated) {
     // the marginal column pass: narrow slabs spread over every SM, row partials summed across
-    // clusters of 8 blocks in distributed shared memory, so that z_blocks stays small
+    // clusters of 4 blocks in distributed shared memory, so that z_blocks stays small
     h->z_lines = std::min(2, aw_col_pass_max_lines(h->nr, h->nc, h->f32));
     const size_t z_smem = (size_t)h->nr * h->z_lines * h->esz + (size_t)h->nr * 16;
-    h->z_cluster = (h->nc / h->z_lines) % 8 == 0 && h->nr % 8 == 0 && z_smem <= 160 * 1024 ? 8 : 1;
+    h->z_cluster = (h->nc / h->z_lines) % 4 == 0 && h->nr % 4 == 0 && z_smem <= 160 * 1024 ? 4 : 1;
     h->z_blocks = h->nc / h->z_lines / h->z_cluster;
     // two parities, so that step n's reduction can run while step n + 1 writes the other
     TRY(dalloc(h->zbuf, 2 * ni * (size_t)(h->nc + h->nr) * 16));

@@ -142,9 +142,10 @@ __device__ __forceinline__ double block_sum(double x, double* red, int tid) {
 }
 
 template <typename V, class Tile, int NT>
-// At most 128 registers a thread (4 blocks of 128 threads, 2 of 256 per SM): the double-float
-// passes are latency-bound, and the occupancy gained beats the few registers they would use beyond.
-__global__ void __launch_bounds__(NT, (NT <= 128 ? 4 : (NT <= 256 ? 2 : 1))) aw_pass_kernel(const __grid_constant__ AwPassArgs a) {
+// Register budget: 5 blocks of 128 threads (96 registers a thread) or 2 blocks of 256 per SM.  The
+// double-float passes are latency-bound and the occupancy gained beats the few spills (measured on
+// the 1024-point passes: 4 blocks 0.180 ms a step, 5 blocks 0.174, 6 blocks 0.183).
+__global__ void __launch_bounds__(NT, (NT <= 128 ? 5 : (NT <= 256 ? 2 : 1))) aw_pass_kernel(const __grid_constant__ AwPassArgs a) {
   extern __shared__ __align__(16) unsigned char aw_smem[];
   typedef typename RealOf<V>::type T;
   V* s = reinterpret_cast<V*>(aw_smem);
