@@ -107,8 +107,14 @@ template <typename V> struct Dft<8, V> {
   }
 };
 
-template <int REM> struct RadixChoice {
-  static constexpr int R = REM >= 8 ? 8 : REM;
+// radix of a stage with REM points left to combine: at most MAXR, the number of elements a thread
+// owns when it is below 8 (every stage then gives each thread whole butterflies)
+template <int REM, int MAXR = 8> struct RadixChoice {
+  static constexpr int R = REM >= MAXR ? MAXR : REM;
+};
+template <class Tile, int NT> struct MaxRadix {
+  static constexpr int E = Tile::N * Tile::LINES / NT;
+  static constexpr int value = E < 8 ? E : 8;
 };
 
 // Middle Stockham stage with span NS: shared memory to shared memory, in place
@@ -116,7 +122,7 @@ template <int REM> struct RadixChoice {
 template <class Tile, int NT, int NS, typename V>
 __device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __restrict__ tw, int tid, unsigned inv) {
   constexpr int N = Tile::N;
-  constexpr int R = RadixChoice<N / NS>::R;
+  constexpr int R = RadixChoice<N / NS, MaxRadix<Tile, NT>::value>::R;
   constexpr int NB = N / R;
   constexpr int TOT = Tile::LINES * NB;
   static_assert(TOT % NT == 0, "work items must divide evenly over the threads");
@@ -148,7 +154,7 @@ __device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __res
 template <class Tile, int NT, int NS, typename V> struct MiddleStages {
   // applies stages NS, NS*R, ... up to but excluding the last one
   __device__ __forceinline__ static void run(V* s, const V* tw, int tid, unsigned inv) {
-    constexpr int R = RadixChoice<Tile::N / NS>::R;
+    constexpr int R = RadixChoice<Tile::N / NS, MaxRadix<Tile, NT>::value>::R;
     if constexpr (NS * R < Tile::N) {
       stockham_stage<Tile, NT, NS, V>(s, tw, tid, inv);
       MiddleStages<Tile, NT, NS * R, V>::run(s, tw, tid, inv);
@@ -156,11 +162,11 @@ template <class Tile, int NT, int NS, typename V> struct MiddleStages {
   }
 };
 
-template <int N, int NS> struct LastSpan {
-  static constexpr int R = RadixChoice<N / NS>::R;
-  static constexpr int value = NS * R >= N ? NS : LastSpan<N, NS * R>::value;
+template <int N, int NS, int MAXR> struct LastSpan {
+  static constexpr int R = RadixChoice<N / NS, MAXR>::R;
+  static constexpr int value = NS * R >= N ? NS : LastSpan<N, NS * R, MAXR>::value;
 };
-template <int N> struct LastSpan<N, N> {
+template <int N, int MAXR> struct LastSpan<N, N, MAXR> {
   static constexpr int value = N;
 };
 
@@ -171,8 +177,9 @@ __device__ __forceinline__ void tile_fft_regs(V* r, V* __restrict__ s, const V* 
   constexpr int N = Tile::N;
   constexpr int L = Tile::LINES;
   constexpr int E = N * L / NT;
-  constexpr int R1 = RadixChoice<N>::R;
-  static_assert(R1 == 8 && E % 8 == 0, "the first stage must be radix 8 over the thread's own elements");
+  constexpr int MAXR = MaxRadix<Tile, NT>::value;
+  constexpr int R1 = RadixChoice<N, MAXR>::R;
+  static_assert(R1 == MAXR && E % R1 == 0, "the first stage combines the thread's own elements");
   constexpr int PER1 = E / R1;
   // the previous use of the tile may still be read by other threads
   __syncthreads();
@@ -191,7 +198,7 @@ __device__ __forceinline__ void tile_fft_regs(V* r, V* __restrict__ s, const V* 
   __syncthreads();
   MiddleStages<Tile, NT, R1, V>::run(s, tw, tid, inv);
   // last stage: span NSL = N / RL; outputs land on the thread's own positions
-  constexpr int NSL = LastSpan<N, R1>::value;
+  constexpr int NSL = LastSpan<N, R1, MAXR>::value;
   constexpr int RL = N / NSL;
   constexpr int NBL = N / RL;
   constexpr int PERL = L * NBL / NT;

@@ -8,6 +8,8 @@
 #pragma once
 #include <cooperative_groups.h>
 
+#include <type_traits>
+
 #include "aw_common.cuh"
 #include "aw_fft.cuh"
 #include "aw_pass.h"
@@ -20,9 +22,14 @@ namespace cg = cooperative_groups;
 // registers a thread).  The number of lines per tile is chosen at run time
 // (aw_row_pass_lines / aw_col_pass_lines) so that a launch spreads over all
 // 152 SMs; column tiles hold at most 4096 elements.
-template <typename V, int N, int LINES> struct Shape {
+// A double-float row of 1024 elements is spread over 256 threads of 4 elements (radix-4 stages, 64
+// registers, 4 blocks a SM): more warps for the latency-bound row pass, whose branch point keeps a
+// second copy of the elements in registers (measured: 0.174 -> 0.170 ms a step; tiles of several
+// shorter rows spill at 64 registers and keep 8 elements a thread).
+template <typename V, int N, int LINES, bool ROW = false> struct Shape {
   static constexpr int TILE = N * LINES;
-  static constexpr int E = TILE / 512 > 8 ? TILE / 512 : 8;
+  static constexpr int E = (ROW && std::is_same<V, dfc>::value && N == 1024 && LINES == 1) ? 4
+                                                                                 : (TILE / 512 > 8 ? TILE / 512 : 8);
   static constexpr int NT = TILE / E;
   // the tile fits the 128 KB a block is given: rows are padded by one element when LINES > 1
   static constexpr bool FITS_ROW = (LINES > 1 ? (N + 1) * LINES : N) * (int)sizeof(V) <= 128 * 1024;
@@ -142,10 +149,13 @@ __device__ __forceinline__ double block_sum(double x, double* red, int tid) {
 }
 
 template <typename V, class Tile, int NT>
-// Register budget: 5 blocks of 128 threads (96 registers a thread) or 2 blocks of 256 per SM.  The
-// double-float passes are latency-bound and the occupancy gained beats the few spills (measured on
-// the 1024-point passes: 4 blocks 0.180 ms a step, 5 blocks 0.174, 6 blocks 0.183).
-__global__ void __launch_bounds__(NT, (NT <= 128 ? 5 : (NT <= 256 ? 2 : 1))) aw_pass_kernel(const __grid_constant__ AwPassArgs a) {
+// Register budget: 5 blocks of 128 threads (96 registers a thread) or 2 blocks of 256 per SM, and 4
+// blocks of 256 (64 registers) for 4 elements a thread.  The double-float passes are latency-bound
+// and the occupancy gained beats the few spills (measured on the 1024-point passes: 4 blocks of 128
+// threads 0.180 ms a step, 5 blocks 0.174, 6 blocks 0.183).
+__global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 1)
+                                                              : (NT <= 128 ? 5 : (NT <= 256 ? 2 : 1))))
+    aw_pass_kernel(const __grid_constant__ AwPassArgs a) {
   extern __shared__ __align__(16) unsigned char aw_smem[];
   typedef typename RealOf<V>::type T;
   V* s = reinterpret_cast<V*>(aw_smem);
@@ -366,7 +376,7 @@ static int prepare_smem(K kern, size_t max_dynamic) {
 
 template <typename V, int N, int LINES>
 static int launch_row_t(const AwPassArgs* a, int batch, cudaStream_t st) {
-  typedef Shape<V, N, LINES> S;
+  typedef Shape<V, N, LINES, true> S;
   if constexpr (!S::FITS_ROW) {
     return -5;
   } else {
