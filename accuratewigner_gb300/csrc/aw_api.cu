@@ -172,6 +172,8 @@ struct aw_state_s {
   DevBuf tabs;                         // phase tables, slots of (nc + nr) complex
   DevBuf vseq, vtimes;                 // time-dependent kick tables of a run of time points, their times
   DevBuf maskx, maskp;                 // 2-D masks (rotated frame)
+  DevBuf maskx2;                       // second x mask of a time-dependent absorber (kicks at t_n, t_n+1)
+  double maskx_t[2] = {NAN, NAN};      // time of the x mask each buffer holds (time-dependent absorber)
   DevBuf red_line, red_cross, red_sq, rowsum, diag, abs2;
   DevBuf scal;                         // device scalars: [0..1] inv_norm (complex), [2..] misc
   DevBuf stop;                         // int
@@ -633,8 +635,8 @@ static int build_tab(aw_state_s* h, int slot, int fn, int mode, double ta, doubl
   return hjit(h, h->k_tab, dim3((n + 31) / 32, count, col_base ? 1 : h->vc), dim3(32), args);
 }
 
-static int build_mask2d(aw_state_s* h, int which, double t) {
-  DevBuf& m = which == 0 ? h->maskx : h->maskp;
+static int build_mask2d(aw_state_s* h, int which, double t, DevBuf* target = nullptr) {
+  DevBuf& m = target ? *target : (which == 0 ? h->maskx : h->maskp);
   void* out = at_inst(m.p, gsz(h), h->f32 ? 4 : 8, h->v0);
   int f32 = tab_fmt(h), nr = h->nr, nc = h->nc;
   double a = h->cfg.dXX, b = h->cfg.dXX_prime, c = h->cfg.dPP, d = h->cfg.dPP_prime;
@@ -1027,6 +1029,7 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   // 2-D absorbing masks of the rotated frame (one per instance)
   if (h->kn.rotated) {
     if (cfg->absx_mode) TRY(dalloc(h->maskx, ni * grid * (h->f32 ? 4 : 8)));
+    if (cfg->absx_mode == 2) TRY(dalloc(h->maskx2, ni * grid * (h->f32 ? 4 : 8)));
     if (cfg->absp_mode) TRY(dalloc(h->maskp, ni * grid * (h->f32 ? 4 : 8)));
   }
 
@@ -1634,12 +1637,24 @@ static int rot_tables_K(aw_state_s* h, const StepPlan& p, double tn) {
   return build_tab(h, TAB_K, 1, 0, tn + 0.5 * c.dt, 0.0, -c.dt, 0.0, 0.0, 0, 0.0);
 }
 
-// V-kick factor; `mask_t` >= 0 evaluates a time-dependent mask at that time
-static int vkick(aw_state_s* h, const StepPlan& p, int slot, bool sign, double t_mask, AwFactor* f) {
+// V-kick factor of time point n (time t_mask = t_n for the absorber, as expV of
+// wigner_moyal_cuda_1d.py:742-760 evaluates abs_boundary_x at the kernel's t).  A time-dependent
+// absorber alternates between two mask buffers by the parity of n, since the row pass applies the
+// kicks of t_n and t_n+1 together; a buffer is rebuilt only when it holds another time.
+static int vkick(aw_state_s* h, const StepPlan& p, int slot, bool sign, double t_mask, AwFactor* f, long long n) {
   *f = ftab(h, p.bloch ? TAB_BV : slot);
   f->sign = sign;
-  if (!p.bloch && h->cfg.absx_mode) {
-    if (h->cfg.absx_mode == 2 || !h->maskx_ready) {
+  if (!p.bloch && h->cfg.absx_mode == 2) {
+    const int b = (int)(n & 1);
+    DevBuf& m = b ? h->maskx2 : h->maskx;
+    if (!(h->maskx_t[b] == t_mask)) {
+      TRY(build_mask2d(h, 0, t_mask, &m));
+      h->maskx_t[b] = t_mask;
+    }
+    f->mask = m.p;
+    f->mask_pow = 1;
+  } else if (!p.bloch && h->cfg.absx_mode) {
+    if (!h->maskx_ready) {
       TRY(build_mask2d(h, 0, t_mask));
       h->maskx_ready = true;
     }
@@ -1654,8 +1669,6 @@ static int vkick(aw_state_s* h, const StepPlan& p, int slot, bool sign, double t
 //   rows of observables go to hist (one per step) when p.ehrenfest.
 static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std::vector<double>& times, double* hist) {
   const aw_config& c = h->cfg;
-  if (!p.bloch && (c.absx_mode == 2 || c.absp_mode == 2))
-    return fail(AW_E_ARG, "time-dependent abs_boundary_x / abs_boundary_p are not supported by the rotated-frame passes");
   const bool vdep = !p.bloch && (c.v_time_dependent || c.absx_mode == 2);
   const bool kdep = !p.bloch && (c.k_time_dependent || c.absp_mode == 2);
   const long long grid = (long long)h->nr * h->nc;
@@ -1687,7 +1700,7 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
   }
   // kick factor of time point n (table slot TAB_V1 when V does not depend on time)
   auto vfactor = [&](long long n, bool sign, AwFactor* f) -> int {
-    TRY(vkick(h, p, TAB_V1, sign, times[n], f));
+    TRY(vkick(h, p, TAB_V1, sign, times[n], f, n));
     if (!vdep) return AW_OK;
     const long long need_hi = std::min(n + 1, steps + 1);
     if (n < vs_n0 || need_hi >= vs_n0 + vs_cnt) {
@@ -2662,6 +2675,7 @@ extern "C" int aw_set_params(aw_handle h, int32_t inst, const double* values) {
   CK(cudaStreamSynchronize(h->st));
   h->minima_ok[inst] = 0;
   h->maskx_ready = h->maskp_ready = false;  // masks may depend on the parameters
+  h->maskx_t[0] = h->maskx_t[1] = NAN;
   return AW_OK;
 }
 

@@ -87,6 +87,30 @@ def test_strong_field_time_dependent_with_absorber():
         assert obs_close(getattr(g, name), getattr(c, name), TOL), name
 
 
+def test_time_dependent_absorbers_in_both_frames():
+    # abs_boundary_x and abs_boundary_p that change with t: the row pass applies the kicks of t_n and
+    # t_n+1 with masks of their own times
+    from accuratewigner_gb300 import WignerMoyalCUDA1D
+    from oracle.propagators import WignerMoyalOracle
+
+    p = dict(WM_STRONG_FIELD)
+    p["abs_boundary_x"] = ("pow(abs(sin(0.5 * M_PI * (XX + XX_max) / XX_max) * sin(0.5 * M_PI * (XX_prime + "
+                           "XX_prime_max) / XX_prime_max)), dt * (0.05 + 0.02 * sin(0.1 * t)))")
+    p["abs_boundary_p"] = "exp(-dt * 0.001 * (1. + cos(0.2 * t)) * (PP * PP + PP_prime * PP_prime))"
+    g = WignerMoyalCUDA1D(**p)
+    c = WignerMoyalOracle(**p, py_functions={"E": e_field})
+    init = "exp(-pow(X - 2., 2) - P * P) / M_PI"
+    g.set_wignerfunction(init)
+    c.set_wignerfunction(init)
+    for n in (7, 13):  # two calls: the masks carry over between them
+        g.propagate(n)
+        c.propagate(n)
+    assert rel_l2(g.wignerfunction.get(), c.wignerfunction) < TOL
+    for name in ("X_average", "P_average", "P_average_RHS", "hamiltonian_average"):
+        assert obs_close(getattr(g, name), getattr(c, name), TOL), name
+    g.close()
+
+
 def test_wigner_bloch_gibbs_matches_oracle_and_analytic():
     from accuratewigner_gb300 import WignerBlochCUDA1D
     from oracle.propagators import WignerBlochOracle
