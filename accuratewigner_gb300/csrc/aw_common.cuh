@@ -114,6 +114,19 @@ template <typename V> __device__ __forceinline__ V cscale(V a, typename scalar_o
   return cmake<V>(a.x * s, a.y * s);
 }
 
+// complex64 on packed FP32 pairs: one FADD2 for a sum, FMUL2 + FFMA2 for a product
+template <> __device__ __forceinline__ float2 cadd<float2>(float2 a, float2 b) { return __fadd2_rn(a, b); }
+template <> __device__ __forceinline__ float2 csub<float2>(float2 a, float2 b) { return __fadd2_rn(a, p_neg(b)); }
+// a b = re(a) (b.x, b.y) + im(a) (-b.y, b.x)
+template <> __device__ __forceinline__ float2 cmul<float2>(float2 a, float2 b) {
+  return __ffma2_rn(p_bcast(a.x), b, __fmul2_rn(p_bcast(a.y), p_rot(b)));
+}
+// a conj(b) = re(a) (b.x, -b.y) + im(a) (b.y, b.x)
+template <> __device__ __forceinline__ float2 cmulc<float2>(float2 a, float2 b) {
+  return __ffma2_rn(p_bcast(a.x), p_conj(b), __fmul2_rn(p_bcast(a.y), p_swap(b)));
+}
+template <> __device__ __forceinline__ float2 cscale<float2>(float2 a, float s) { return __fmul2_rn(a, p_bcast(s)); }
+
 template <> __device__ __forceinline__ dfc cadd<dfc>(dfc a, dfc b) { return dfc_add(a, b); }
 template <> __device__ __forceinline__ dfc csub<dfc>(dfc a, dfc b) { return dfc_sub(a, b); }
 template <> __device__ __forceinline__ dfc cmul<dfc>(dfc a, dfc b) { return dfc_mul(a, b); }
