@@ -16,8 +16,9 @@
 //
 // Data placement.  Each thread owns E elements of the tile, all on one line:
 //   line = tid % LINES,  position p_k = tid / LINES + k * (N / E),  k = 0..E-1.
-// The first Stockham stage (span 1) of radix 8 reads exactly these elements
-// and the last stage writes exactly these positions, so an FFT starts from
+// Every stage has radix min(8, E) (less for the remainder), so the first
+// Stockham stage (span 1) reads exactly these elements and the last stage
+// writes exactly these positions, so an FFT starts from
 // and ends in registers; only the stages in between go through shared memory
 // (read all inputs, synchronise, write all outputs).  Element-wise factors,
 // global loads and stores and reductions all work on the registers.
