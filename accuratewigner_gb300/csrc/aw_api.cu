@@ -1066,7 +1066,7 @@ extern "C" int aw_destroy(aw_handle h) {
                     &h->vseq, &h->vtimes, &h->zbuf, &h->altbuf, &h->twist_hi, &h->twist_lo, &h->rho, &h->W, &h->snap, &h->tmp, &h->stage, &h->tw_r, &h->tw_c, &h->tw_w, &h->shx_hi,
                     &h->shx_lo, &h->shy_hi, &h->shy_lo, &h->tabs, &h->maskx, &h->maskp, &h->red_line,
                     &h->red_cross, &h->red_sq, &h->rowsum, &h->diag, &h->abs2, &h->scal, &h->stop, &h->hist,
-                    &h->terms, &h->part, &h->blk_tabs};
+                    &h->terms, &h->part, &h->blk_tabs, &h->params, &h->bvec, &h->maskx2};
   for (DevBuf* b : bufs) dfree(*b);
   for (DevBuf& b : h->sw_states) dfree(b);
   if (h->st) cudaStreamDestroy(h->st);
