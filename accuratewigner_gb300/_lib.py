@@ -112,6 +112,7 @@ SIGNATURES = [
     ("aw_rho2wigner", c_int, [c_vp, c_int]),
     ("aw_normalize_rho_wigner", c_int, [c_vp]),
     ("aw_propagate", c_int, [c_vp, c_i64, ctypes.POINTER(c_dbl)]),
+    ("aw_single_step", c_int, [c_vp, c_dbl]),
     ("aw_history", c_int, [c_vp, c_vp, c_i64, ctypes.POINTER(c_i64), ctypes.POINTER(c_int)]),
     ("aw_average", c_int, [c_vp, c_cp, c_dbl, ctypes.POINTER(c_dbl)]),
     ("aw_average_ops", c_int, [c_vp, ctypes.POINTER(c_cp), c_int, c_dbl, ctypes.POINTER(c_dbl)]),
@@ -123,6 +124,7 @@ SIGNATURES = [
     ("aw_sw_clear_states", c_int, [c_vp]),
     ("aw_sw_get_state", c_int, [c_vp, c_int, c_vp]),
     ("aw_sw_energy", c_int, [c_vp, c_dbl, ctypes.POINTER(c_dbl)]),
+    ("aw_sw_ehrenfest", c_int, [c_vp, c_dbl, ctypes.POINTER(c_dbl)]),
     ("aw_reduce_noalloc", c_int, [c_vp, c_int, c_i64, c_i64, c_int, c_vp, c_vp]),
     ("aw_set_view", c_int, [c_vp, c_int, c_int]),
     ("aw_set_params", c_int, [c_vp, c_int, ctypes.POINTER(c_dbl)]),

@@ -1854,6 +1854,22 @@ extern "C" int aw_propagate(aw_handle h, int64_t steps, double* t) {
   return AW_OK;
 }
 
+// One split step at time t, as single_step_propagation does it (wigner_moyal_cuda_1d.py:543-561,
+// rho_vneumann_cuda_1d.py:450-468, schrodinger_wigner_cuda_1d.py:356-369): V and K at the kernels'
+// times for t, not normalised, no observables, t unchanged.
+int vn_single_step(aw_state_s* h, double t);
+int sw_single_step(aw_state_s* h, double t);
+extern "C" int aw_single_step(aw_handle h, double t) {
+  if (!h) return fail(AW_E_ARG, "null handle");
+  Settled guard{h};
+  TRY(clear_stops(h));
+  if (h->kn.vn) return vn_single_step(h, t);
+  if (h->kn.sw) return sw_single_step(h, t);
+  const std::vector<double> times{t - h->cfg.dt, t, t + h->cfg.dt};
+  StepPlan p{false, 0.0, false, false, 0};
+  return rot_run(h, p, 1, times, nullptr);
+}
+
 extern "C" int aw_history_of(aw_handle h, int32_t inst, double* out, int64_t max_rows, int64_t* rows, int32_t* cols) {
   if (!h) return fail(AW_E_ARG, "null handle");
   if (inst < 0 || inst >= h->ni) return fail(AW_E_ARG, "no instance %d", inst);
@@ -2187,6 +2203,12 @@ int vn_propagate(aw_state_s* h, long long steps, double* t) {
   return AW_OK;
 }
 
+int vn_single_step(aw_state_s* h, double t) {
+  const std::vector<double> times{t - h->cfg.dt, t, t + h->cfg.dt};
+  VnPlan p{false, 0.0, false, false, 0, 0};
+  return vn_run(h, p, 1, times, nullptr, h->hist_cols);
+}
+
 int vn_bloch_step(aw_state_s* h, double dbeta, double* out) {
   if (h->ni > 1) return fail(AW_E_STATE, "single rho-Bloch steps need a single propagator (use aw_gibbs_batch)");
   TRY(ensure_hist(h, 2));
@@ -2492,6 +2514,30 @@ int sw_propagate(aw_state_s* h, long long steps, double* t) {
   KL(aw_k_scale(h->rho.p, h->f32, h->nc, 1.0, 0.0, dinv(h), h->st));
   h->hist_rows = c.ehrenfest ? steps : 0;
   *t = times[steps];
+  return AW_OK;
+}
+
+int sw_single_step(aw_state_s* h, double t) {
+  TRY(sw_tables(h, t));
+  const AwFactor pre = sw_tab(h, TAB_V1, 1), mid = sw_tab(h, TAB_K, 2), post = sw_tab(h, TAB_V1, 1);
+  return sw_run(h, h->rho.p, h->rho.p, pre, mid, post, false, nullptr, nullptr);
+}
+
+// get_Ehrenfest of the Schrodinger propagator (schrodinger_wigner_cuda_1d.py:412-459) for the
+// current wave function at time t: one row of observables (n_slots + 2 values).  The observables
+// are ratios to the norms of psi and of its momentum representation, so psi itself is left as it
+// is (the reference rescales it to sqrt(N) psi / |psi| on the way).
+extern "C" int aw_sw_ehrenfest(aw_handle h, double t, double* row) {
+  if (!h || !row) return fail(AW_E_ARG, "null argument");
+  if (!h->kn.sw) return fail(AW_E_STATE, "aw_sw_ehrenfest needs the Schrodinger propagator");
+  if (!h->cfg.ehrenfest) return fail(AW_E_STATE, "the propagator records no Ehrenfest observables");
+  Settled guard{h};
+  TRY(ensure_hist(h, 1));
+  CK(cudaMemcpyAsync(h->W.p, h->rho.p, (size_t)h->sw_rows * h->nc * h->esz, cudaMemcpyDeviceToDevice, h->st));
+  TRY(sw_run(h, h->rho.p, h->tmp.p, fnone(), fnone(), fnone(), true, nullptr, nullptr));
+  TRY(sw_finalize(h, t, (double*)h->hist.p));
+  CK(cudaMemcpyAsync(row, h->hist.p, (size_t)h->hist_cols * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
   return AW_OK;
 }
 

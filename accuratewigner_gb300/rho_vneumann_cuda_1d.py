@@ -179,6 +179,11 @@ class RhoVNeumannCUDA1D:
             _lib.check(lib.aw_history(self._h, out.ctypes.data_as(_c.c_void_p), n, None, None))
         return out
 
+    def single_step_propagation(self):
+        """One split step at the current self.t (vn:450-468); rho is not normalised."""
+        _lib.check(_lib.load().aw_single_step(self._h, float(self.t)))
+        return self.rho
+
     def propagate(self, steps=1):
         lib = _lib.load()
         if self.isEhrenfest and not self._native_ehrenfest:

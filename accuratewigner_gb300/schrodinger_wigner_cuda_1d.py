@@ -116,6 +116,7 @@ class SchrodingerWignerCUDA1D:
         cfg.absp_mode = mask_mode(info, self.abs_boundary_p)
         cfg.ehrenfest = int(bool(self._native_ehrenfest and self.isEhrenfest))
         (table if self._native_ehrenfest else TermTable(info)).fill(cfg, keep)
+        self._n_slots = int(cfg.n_slots)
         self._handle = Handle(cfg)
         self._h = self._handle._h
 
@@ -150,6 +151,26 @@ class SchrodingerWignerCUDA1D:
         return self
 
     # ------------------------------------------------------------------ propagation (sw:356-459)
+    def single_step_propagation(self):
+        """One split step at the current self.t (sw:356-369); the wave function is not normalised."""
+        _lib.check(_lib.load().aw_single_step(self._h, float(self.t)))
+        return self.wavefunction
+
+    def get_Ehrenfest(self, t):
+        """Append the Ehrenfest observables of the current wave function at time t (sw:412-459)."""
+        if not self.isEhrenfest:
+            return
+        if not self._native_ehrenfest:
+            raise NotImplementedError("Ehrenfest observables must be functions of X or of P alone")
+        row = np.empty(self._n_slots + 2, np.float64)
+        _lib.check(_lib.load().aw_sw_ehrenfest(self._h, float(t), row.ctypes.data_as(_c.POINTER(_c.c_double))))
+        s = self._ehrenfest_slots
+        self.X_average.append(float(row[s[0]]))
+        self.X_average_RHS.append(float(row[s[1]]))
+        self.P_average.append(float(row[s[2]]))
+        self.P_average_RHS.append(float(row[s[3]]))
+        self.hamiltonian_average.append(float(row[s[4]]))
+
     def propagate(self, steps=1):
         lib = _lib.load()
         if self.isEhrenfest and not self._native_ehrenfest:
@@ -202,6 +223,23 @@ class SchrodingerWignerCUDA1D:
             _lib.check(lib.aw_sw_store_state(self._h))
         self._n_states = nstates
         return self
+
+    def projectout_stationary_states(self, wavefunction):
+        """The wave function normalised, with its projections on the stored stationary states removed
+        and normalised again (sw:505-550; unweighted scalar products and norms, as there).  Accepts
+        a host array or a device array of this package; returns the same kind of object."""
+        dev = hasattr(wavefunction, "get") and not isinstance(wavefunction, np.ndarray)
+        psi = np.array(wavefunction.get() if dev else wavefunction, dtype=np.complex128)
+        psi /= np.linalg.norm(psi)
+        states = self.stationary_states
+        projs = [np.vdot(phi, psi) for phi in states]
+        for phi, c in zip(states, projs):
+            psi -= c * phi.reshape(psi.shape)
+        psi /= np.linalg.norm(psi)
+        if dev:
+            wavefunction.set(psi)
+            return wavefunction
+        return psi
 
     @property
     def stationary_states(self):

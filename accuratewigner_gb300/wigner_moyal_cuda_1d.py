@@ -245,6 +245,12 @@ class WignerMoyalCUDA1D:
         for lst, slot in zip(self.extra_average, self._extra_slots):
             lst.extend(rows[:, slot].tolist())
 
+    def single_step_propagation(self):
+        """One split step at the current self.t (wm:543-561); rho is not normalised and W is not
+        updated."""
+        _lib.check(_lib.load().aw_single_step(self._h, float(self.t)))
+        return self.rho
+
     def propagate(self, steps=1):
         lib = _lib.load()
         if (self.isEhrenfest or self.extra_observables) and not self._native_ehrenfest:

@@ -187,6 +187,10 @@ int aw_normalize_rho_wigner(aw_handle h);
  * *t holds the time before the call and receives the time after it, accumulated
  * step by step in FP64 exactly as the reference's `self.t += self.dt`. */
 int aw_propagate(aw_handle h, int64_t steps, double* t);
+/* One split step at time t exactly as single_step_propagation (wigner_moyal_cuda_1d.py:543-561,
+ * rho_vneumann_cuda_1d.py:450-468, schrodinger_wigner_cuda_1d.py:356-369): not normalised, no
+ * observables, the time left to the caller. */
+int aw_single_step(aw_handle h, double t);
 /* Observables recorded by the last aw_propagate: rows x (n_slots + 2) doubles,
  * columns = slots, purity, norm. */
 int aw_history(aw_handle h, double* out, int64_t max_rows, int64_t* rows, int32_t* cols);
@@ -221,6 +225,9 @@ int aw_sw_store_state(aw_handle h);                 /* append psi to the station
 int aw_sw_clear_states(aw_handle h);                /* forget the stored stationary states */
 int aw_sw_get_state(aw_handle h, int32_t index, void* dst_host);
 int aw_sw_energy(aw_handle h, double t, double* out); /* get_energy, sw:461-482 */
+/* get_Ehrenfest, sw:412-459: the observable row (n_slots + 2 doubles) of the current wave function
+ * at time t; the wave function is left unchanged */
+int aw_sw_ehrenfest(aw_handle h, double t, double* row);
 
 /* Buffer reduction that allocates nothing (no counterpart in the reference).
  * For callers that cannot allocate device memory: a host application that owns
