@@ -295,8 +295,9 @@ def run_ours(args):
                 "frac": (achieved / peak) if achieved else None,
                 "traffic": traffic,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s",
-                "note": "the passes are bound by arithmetic (FP64 pipe, or FP32 issue for double-float), not HBM; "
-                        "frac is the HBM fraction of the dominant pass",
+                "note": "the passes are bound by the latency and FP32 issue of their double-float arithmetic "
+                        "(native FP64: by the FP64 pipe), not by HBM; the 48 MB working set stays in L2 within a "
+                        "call; frac is the HBM fraction of the dominant pass",
             },
             "kernel_profile": prof,
             "clocks": clk.summary(),
