@@ -279,8 +279,8 @@ def run_ours(args):
                 "precision": args.precision,
                 "grid": [N_GRID, N_GRID],
                 "steps_per_call": CHUNK,
-                "l2": "flushed (256 MB write) before every timed propagate() call; the 32 MB state stays "
-                      "L2-resident within a call",
+                "l2": "flushed (256 MB write) before every timed propagate() call; the 48 MB working set "
+                      "(state and two branch buffers) stays L2-resident within a call",
                 "parallelism": "replicas" if world > 1 else "single GPU",
                 "algorithmic_bytes_per_pt_step": ALG_BYTES_FACTOR * S,
             },
