@@ -133,19 +133,26 @@ __device__ __forceinline__ void store_regs(V* __restrict__ dst, const V* r, int 
   }
 }
 
-// deterministic block sum of one double per thread (NT a power of two); result valid in thread 0
+// deterministic block sum of one double per thread (NT a power of two); result valid in thread 0:
+// a fixed shuffle tree inside each warp, then the warp sums in index order (two barriers instead of
+// one per halving)
 template <int NT>
 __device__ __forceinline__ double block_sum(double x, double* red, int tid) {
-  red[tid] = x;
-  __syncthreads();
-#pragma unroll 1
-  for (int w = NT / 2; w > 0; w >>= 1) {
-    if (tid < w) red[tid] += red[tid + w];
+  constexpr int W = NT < 32 ? NT : 32;
+#pragma unroll
+  for (int o = W / 2; o > 0; o >>= 1) x += __shfl_down_sync(lane_mask<NT>(), x, o, W);
+  if constexpr (NT <= 32) {
+    return x;
+  } else {
+    if ((tid & 31) == 0) red[tid >> 5] = x;
     __syncthreads();
+    double out = 0.0;
+    if (tid == 0)
+#pragma unroll
+      for (int w = 0; w < NT / 32; ++w) out += red[w];
+    __syncthreads();
+    return out;
   }
-  const double out = red[0];
-  __syncthreads();
-  return out;
 }
 
 template <typename V, class Tile, int NT>
