@@ -67,6 +67,9 @@ template <typename V> struct cpart {
   __device__ static double2 zero() { return make_double2(0.0, 0.0); }
   __device__ static double2 add(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
   __device__ static double2 to_d2(double2 a) { return a; }
+  __device__ static double2 shfl_xor(unsigned m, double2 a, int o, int w) {
+    return make_double2(__shfl_xor_sync(m, a.x, o, w), __shfl_xor_sync(m, a.y, o, w));
+  }
 };
 template <> struct cpart<dfc> {
   typedef dfc type;
@@ -74,6 +77,10 @@ template <> struct cpart<dfc> {
   __device__ static dfc zero() { return dfc{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}; }
   __device__ static dfc add(dfc a, dfc b) { return dfc_add(a, b); }
   __device__ static double2 to_d2(dfc a) { return dfc_to_double2(a); }
+  __device__ static dfc shfl_xor(unsigned m, dfc a, int o, int w) {
+    return dfc{make_float2(__shfl_xor_sync(m, a.h.x, o, w), __shfl_xor_sync(m, a.h.y, o, w)),
+               make_float2(__shfl_xor_sync(m, a.l.x, o, w), __shfl_xor_sync(m, a.l.y, o, w))};
+  }
 };
 
 template <typename V>

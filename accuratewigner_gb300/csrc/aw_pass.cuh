@@ -274,12 +274,18 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
         }
       }
       if (a.col_alt) {
-        cred[tid] = cpart<V>::make(cr, ci);
+        // the lanes of one column in a warp (equal lane mod B) by a fixed shuffle tree, then the
+        // warps in index order
+        constexpr int W = NT < 32 ? NT : 32;
+        typename cpart<V>::type acc = cpart<V>::make(cr, ci);
+#pragma unroll
+        for (int o = W / 2; o >= B; o >>= 1) acc = cpart<V>::add(acc, cpart<V>::shfl_xor(lane_mask<NT>(), acc, o, W));
+        if ((tid % W) < B) cred[(tid / W) * B + (tid % W)] = acc;
         __syncthreads();
         if (tid < B) {
-          typename cpart<V>::type acc = cpart<V>::zero();
-          for (int m = tid; m < NT; m += B) acc = cpart<V>::add(acc, cred[m]);
-          a.col_alt[(long long)inst * ncols + line0 + tid] = cpart<V>::to_d2(acc);
+          typename cpart<V>::type sum = cpart<V>::zero();
+          for (int w = 0; w < NT / W; ++w) sum = cpart<V>::add(sum, cred[w * B + tid]);
+          a.col_alt[(long long)inst * ncols + line0 + tid] = cpart<V>::to_d2(sum);
         }
         __syncthreads();
       }
@@ -318,12 +324,17 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
         }
       }
       if (a.red_line) {
-        red[tid] = to_d(lsum);
+        // as the marginal sums: shuffle tree over a column's lanes, then the warps in order
+        constexpr int W = NT < 32 ? NT : 32;
+        double acc = to_d(lsum);
+#pragma unroll
+        for (int o = W / 2; o >= B; o >>= 1) acc += __shfl_xor_sync(lane_mask<NT>(), acc, o, W);
+        if ((tid % W) < B) red[(tid / W) * B + (tid % W)] = acc;
         __syncthreads();
         if (tid < B) {
-          double acc = 0.0;
-          for (int m = tid; m < NT; m += B) acc += red[m];
-          a.red_line[(long long)inst * ncols + line0 + tid] = acc;
+          double sum = 0.0;
+          for (int w = 0; w < NT / W; ++w) sum += red[w * B + tid];
+          a.red_line[(long long)inst * ncols + line0 + tid] = sum;
         }
         __syncthreads();
       }
