@@ -84,15 +84,15 @@ __device__ inline float4 aw_df2(double aw_re, double aw_im) {
 __device__ inline double2 aw_load(const void* aw_p, long long aw_k, int aw_f32) {
   if (aw_f32) { float2 aw_v = ((const float2*)aw_p)[aw_k]; return make_double2(aw_v.x, aw_v.y); }
   return ((const double2*)aw_p)[aw_k]; }
+// block sum for blocks of whole warps: a fixed shuffle tree in each warp, then every thread adds the
+// warp sums in index order (the same value in every thread)
 __device__ inline double aw_block_sum(double aw_v, double* aw_red) {
   const int aw_t = threadIdx.x;
-  aw_red[aw_t] = aw_v;
+  for (int aw_o = 16; aw_o > 0; aw_o >>= 1) aw_v += __shfl_down_sync(0xffffffffu, aw_v, aw_o);
+  if ((aw_t & 31) == 0) aw_red[aw_t >> 5] = aw_v;
   __syncthreads();
-  for (int aw_w = blockDim.x / 2; aw_w > 0; aw_w >>= 1) {
-    if (aw_t < aw_w) aw_red[aw_t] += aw_red[aw_t + aw_w];
-    __syncthreads();
-  }
-  double aw_r = aw_red[0];
+  double aw_r = 0.0;
+  for (int aw_w = 0; aw_w < (int)(blockDim.x >> 5); ++aw_w) aw_r += aw_red[aw_w];
   __syncthreads();
   return aw_r;
 }
