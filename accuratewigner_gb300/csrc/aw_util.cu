@@ -37,6 +37,18 @@ __device__ __forceinline__ void st(void* p, long long k, int f32, double2 v) {
   }
 }
 
+// sum of one value per thread over a block of whole warps: a fixed shuffle tree in each warp, then
+// the warp sums in index order; the same result in every thread
+__device__ __forceinline__ double blk_sum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double r = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += sh[w];
+  __syncthreads();
+  return r;
+}
+
 // a *= (re + i im) * ptr[2 inst .. 2 inst + 1]; instance inst = blockIdx.y holds n elements
 __global__ void k_scale(void* a, int f32, long long n, double re, double im, const double* ptr) {
   const long long inst = blockIdx.y;
@@ -77,18 +89,8 @@ __global__ void k_partial(const void* a, int f32, long long n, int mode, long lo
       sr += v.x * v.x + v.y * v.y;
     }
   }
-  const int t = threadIdx.x;
-  rr[t] = sr;
-  ri[t] = si;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (t < w) {
-      rr[t] += rr[t + w];
-      ri[t] += ri[t + w];
-    }
-    __syncthreads();
-  }
-  if (t == 0) part[blockIdx.x] = make_double2(rr[0], ri[0]);
+  const double tr = blk_sum(sr, rr), ti = blk_sum(si, ri);
+  if (threadIdx.x == 0) part[blockIdx.x] = make_double2(tr, ti);
 }
 
 __global__ void k_embed(const void* rho, int f32, int N, void* W, int M, int pad) {
@@ -138,25 +140,16 @@ __global__ void k_trace_finalize(const double2* diag, int n, const double* abs2p
   }
   if (abs2part)
     for (int k = t; k < nparts; k += blockDim.x) sa += abs2part[k];
-  rr[t] = sr;
-  ri[t] = si;
-  ra[t] = sa;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (t < w) {
-      rr[t] += rr[t + w];
-      ri[t] += ri[t + w];
-      ra[t] += ra[t + w];
-    }
-    __syncthreads();
-  }
+  sr = blk_sum(sr, rr);
+  si = blk_sum(si, ri);
+  sa = blk_sum(sa, ra);
   if (t == 0) {
-    const double tr = rr[0] * dX, ti = complex_trace ? ri[0] * dX : 0.0;
+    const double tr = sr * dX, ti = complex_trace ? si * dX : 0.0;
     const double d = tr * tr + ti * ti;
     const double ir = tr / d, ii = -ti / d;
     inv_out[0] = ir;
     inv_out[1] = ii;
-    const double purity = ra[0] * (ir * ir + ii * ii) * dX * dX;
+    const double purity = sa * (ir * ir + ii * ii) * dX * dX;
     if (hist) {
       hist[0] = purity;
       hist[1] = tr;
@@ -173,16 +166,11 @@ __global__ void k_norm_finalize(const double* parts, int nparts, double scale, d
   const int t = threadIdx.x;
   double s = 0.0;
   for (int k = t; k < nparts; k += blockDim.x) s += parts[k];
-  r[t] = s;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (t < w) r[t] += r[t + w];
-    __syncthreads();
-  }
+  s = blk_sum(s, r);
   if (t == 0) {
-    inv_out[0] = 1.0 / sqrt(r[0] * scale);
+    inv_out[0] = 1.0 / sqrt(s * scale);
     inv_out[1] = 0.0;
-    if (hist) hist[0] = r[0];
+    if (hist) hist[0] = s;
   }
 }
 
@@ -212,18 +200,8 @@ __global__ void k_vdot(const void* a, const void* b, int f32, long long n, doubl
     sr += x.x * y.x + x.y * y.y;
     si += x.x * y.y - x.y * y.x;
   }
-  const int t = threadIdx.x;
-  rr[t] = sr;
-  ri[t] = si;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (t < w) {
-      rr[t] += rr[t + w];
-      ri[t] += ri[t + w];
-    }
-    __syncthreads();
-  }
-  if (t == 0) part[blockIdx.x] = make_double2(rr[0], ri[0]);
+  const double tr = blk_sum(sr, rr), ti = blk_sum(si, ri);
+  if (threadIdx.x == 0) part[blockIdx.x] = make_double2(tr, ti);
 }
 
 // y += (cr + i ci) x  (the reference's projectout ElementwiseKernel with C = -proj, sw:532-535)
