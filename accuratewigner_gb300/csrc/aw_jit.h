@@ -363,8 +363,17 @@ extern "C" __global__ void aw_finalize_rot(const double2* aw_z, const double2* a
       for (int aw_i = aw_lo + aw_t; aw_i < aw_lo + aw_len; aw_i += aw_nt) {
         const double P = aw_dP * ((aw_size_t)aw_i - 0.5 * aw_nrow);
         const int aw_k = (aw_nrow - aw_i) & (aw_nrow - 1);
-        double aw_w = 0.0;
-        for (int aw_p = 0; aw_p < aw_nparts; ++aw_p) aw_w += aw_wpart[(long long)aw_p * aw_nrow + aw_k].x;
+        // the partials of w_k in four interleaved sums (loads in flight together), added in a fixed order
+        double aw_w0 = 0.0, aw_w1 = 0.0, aw_w2 = 0.0, aw_w3 = 0.0;
+        int aw_p = 0;
+        for (; aw_p + 4 <= aw_nparts; aw_p += 4) {
+          aw_w0 += aw_wpart[(long long)aw_p * aw_nrow + aw_k].x;
+          aw_w1 += aw_wpart[(long long)(aw_p + 1) * aw_nrow + aw_k].x;
+          aw_w2 += aw_wpart[(long long)(aw_p + 2) * aw_nrow + aw_k].x;
+          aw_w3 += aw_wpart[(long long)(aw_p + 3) * aw_nrow + aw_k].x;
+        }
+        for (; aw_p < aw_nparts; ++aw_p) aw_w0 += aw_wpart[(long long)aw_p * aw_nrow + aw_k].x;
+        const double aw_w = (aw_w0 + aw_w1) + (aw_w2 + aw_w3);
         aw_s += ((aw_i & 1) ? -1.0 : 1.0) * aw_nrow * aw_w * aw_obs_p(aw_idx, P, t, aw_prm);
       }
     }
