@@ -173,6 +173,8 @@ struct aw_state_s {
   DevBuf vseq, vtimes;                 // time-dependent kick tables of a run of time points, their times
   DevBuf maskx, maskp;                 // 2-D masks (rotated frame)
   DevBuf maskx2;                       // second x mask of a time-dependent absorber (kicks at t_n, t_n+1)
+  DevBuf masksep;                      // a separable x mask as column and row factors (nc + nr doubles)
+  bool maskx_sep = false;              // ... folded into the V-kick tables instead of read per point
   double maskx_t[2] = {NAN, NAN};      // time of the x mask each buffer holds (time-dependent absorber)
   DevBuf red_line, red_cross, red_sq, rowsum, diag, abs2;
   DevBuf scal;                         // device scalars: [0..1] inv_norm (complex), [2..] misc
@@ -1066,7 +1068,7 @@ extern "C" int aw_destroy(aw_handle h) {
                     &h->vseq, &h->vtimes, &h->zbuf, &h->altbuf, &h->twist_hi, &h->twist_lo, &h->rho, &h->W, &h->snap, &h->tmp, &h->stage, &h->tw_r, &h->tw_c, &h->tw_w, &h->shx_hi,
                     &h->shx_lo, &h->shy_hi, &h->shy_lo, &h->tabs, &h->maskx, &h->maskp, &h->red_line,
                     &h->red_cross, &h->red_sq, &h->rowsum, &h->diag, &h->abs2, &h->scal, &h->stop, &h->hist,
-                    &h->terms, &h->part, &h->blk_tabs, &h->params, &h->bvec, &h->maskx2};
+                    &h->terms, &h->part, &h->blk_tabs, &h->params, &h->bvec, &h->maskx2, &h->masksep};
   for (DevBuf* b : bufs) dfree(*b);
   for (DevBuf& b : h->sw_states) dfree(b);
   if (h->st) cudaStreamDestroy(h->st);
@@ -1612,6 +1614,9 @@ static AwFactor ftab(aw_state_s* h, int slot) {
   return f;
 }
 
+static int prepare_maskx(aw_state_s* h);
+static int fold_maskx(aw_state_s* h, void* col, int count);
+
 static int rot_tables_V(aw_state_s* h, const StepPlan& p, double tn, double tn1, bool pair) {
   const aw_config& c = h->cfg;
   if (p.bloch) {
@@ -1622,8 +1627,13 @@ static int rot_tables_V(aw_state_s* h, const StepPlan& p, double tn, double tn1,
     return build_tab(h, TAB_BV, 0, 1, c.t_initial, 0.0, -0.25 * p.dbeta, 0.0, 0.5 * h->V_min, 0, 0.0);
   }
   const double half = 0.5 * c.dt;
+  if (c.absx_mode == 1) TRY(prepare_maskx(h));
   TRY(build_tab(h, TAB_V1, 0, 0, tn + half, 0.0, -half, 0.0, 0.0, 0, 0.0));
-  if (pair) TRY(build_tab(h, TAB_V1B, 0, 0, tn1 + half, 0.0, -half, 0.0, 0.0, 0, 0.0));
+  TRY(fold_maskx(h, tab_col(h, TAB_V1), 1));
+  if (pair) {
+    TRY(build_tab(h, TAB_V1B, 0, 0, tn1 + half, 0.0, -half, 0.0, 0.0, 0, 0.0));
+    TRY(fold_maskx(h, tab_col(h, TAB_V1B), 1));
+  }
   return AW_OK;
 }
 
@@ -1635,6 +1645,60 @@ static int rot_tables_K(aw_state_s* h, const StepPlan& p, double tn) {
   if (p.bloch)
     return build_tab(h, TAB_BK, 1, 1, c.t_initial, 0.0, -0.5 * p.dbeta, 0.0, 0.5 * h->K_min, 0, 0.0);
   return build_tab(h, TAB_K, 1, 0, tn + 0.5 * c.dt, 0.0, -c.dt, 0.0, 0.0, 0, 0.0);
+}
+
+// The time-independent x mask of a single propagator, built once.  The reference evaluates
+// abs_boundary_x(XX, XX') per point inside every kick; when the mask is a product f(XX) g(XX') (the
+// usual absorber, e.g. cos(...XX...) * cos(...XX_prime...)) its factors are folded into the column
+// and row tables of the V kick instead, so that the passes read no mask.  The test is numerical:
+// every point within a few rounding errors of m[i, j0] m[i0, j] / m[i0, j0].
+static int prepare_maskx(aw_state_s* h) {
+  if (h->maskx_ready) return AW_OK;
+  TRY(build_mask2d(h, 0, 0.0));
+  h->maskx_ready = true;
+  h->maskx_sep = false;
+  if (h->ni != 1) return AW_OK;
+  const int nr = h->nr, nc = h->nc;
+  const size_t n = (size_t)nr * nc;
+  std::vector<double> m(n);
+  if (h->f32) {
+    std::vector<float> f(n);
+    CK(cudaMemcpy(f.data(), h->maskx.p, n * 4, cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < n; ++k) m[k] = f[k];
+  } else if (h->df) {
+    std::vector<float> f(2 * n);
+    CK(cudaMemcpy(f.data(), h->maskx.p, n * 8, cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < n; ++k) m[k] = (double)f[2 * k] + (double)f[2 * k + 1];
+  } else {
+    CK(cudaMemcpy(m.data(), h->maskx.p, n * 8, cudaMemcpyDeviceToHost));
+  }
+  size_t piv = 0;
+  for (size_t k = 1; k < n; ++k)
+    if (std::fabs(m[k]) > std::fabs(m[piv])) piv = k;
+  const double mx = std::fabs(m[piv]);
+  if (!(mx > 0.0) || !std::isfinite(mx)) return AW_OK;
+  const int i0 = (int)(piv / nc), j0 = (int)(piv % nc);
+  const double tol = (h->f32 ? 1e-6 : 3e-14) * mx;
+  for (int i = 0; i < nr; ++i) {
+    const double u = m[(size_t)i * nc + j0] / m[piv];
+    for (int j = 0; j < nc; ++j)
+      if (!(std::fabs(u * m[(size_t)i0 * nc + j] - m[(size_t)i * nc + j]) <= tol)) return AW_OK;
+  }
+  std::vector<double> sv(nc + nr);
+  for (int j = 0; j < nc; ++j) sv[j] = m[(size_t)i0 * nc + j];
+  for (int i = 0; i < nr; ++i) sv[nc + i] = m[(size_t)i * nc + j0] / m[piv];
+  TRY(dalloc(h->masksep, sv.size() * sizeof(double)));
+  CK(cudaMemcpy(h->masksep.p, sv.data(), sv.size() * sizeof(double), cudaMemcpyHostToDevice));
+  h->maskx_sep = true;
+  return AW_OK;
+}
+
+// folds a separable x mask into `count` V-kick tables at `col` (nc + nr entries each, consecutive)
+static int fold_maskx(aw_state_s* h, void* col, int count) {
+  if (!h->maskx_sep) return AW_OK;
+  KL(aw_k_scale_lines(col, tab_fmt(h), (const double*)h->masksep.p, h->nc + h->nr, count,
+                      (long long)h->nc + h->nr, h->st));
+  return AW_OK;
 }
 
 // V-kick factor of time point n (time t_mask = t_n for the absorber, as expV of
@@ -1654,12 +1718,11 @@ static int vkick(aw_state_s* h, const StepPlan& p, int slot, bool sign, double t
     f->mask = m.p;
     f->mask_pow = 1;
   } else if (!p.bloch && h->cfg.absx_mode) {
-    if (!h->maskx_ready) {
-      TRY(build_mask2d(h, 0, t_mask));
-      h->maskx_ready = true;
+    TRY(prepare_maskx(h));
+    if (!h->maskx_sep) {
+      f->mask = h->maskx.p;
+      f->mask_pow = 1;
     }
-    f->mask = h->maskx.p;
-    f->mask_pow = 1;
   }
   return AW_OK;
 }
@@ -1712,6 +1775,7 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       const double half = 0.5 * c.dt;
       TRY(build_tab(h, 0, 0, 0, half, 0.0, -half, 0.0, 0.0, 0, 0.0, h->vseq.p, (const double*)h->vtimes.p,
                     (int)vs_cnt));
+      TRY(fold_maskx(h, h->vseq.p, (int)vs_cnt));
     }
     f->col_tab = (char*)h->vseq.p + (size_t)(n - vs_n0) * (h->nc + h->nr) * h->esz;
     f->row_tab = (char*)f->col_tab + (size_t)h->nc * h->esz;
@@ -2721,6 +2785,7 @@ extern "C" int aw_set_params(aw_handle h, int32_t inst, const double* values) {
   CK(cudaStreamSynchronize(h->st));
   h->minima_ok[inst] = 0;
   h->maskx_ready = h->maskp_ready = false;  // masks may depend on the parameters
+  h->maskx_sep = false;
   h->maskx_t[0] = h->maskx_t[1] = NAN;
   return AW_OK;
 }

@@ -64,6 +64,16 @@ __global__ void k_scale(void* a, int f32, long long n, double re, double im, con
   }
 }
 
+// tables t = 0 .. count-1 of n complex entries, `stride` entries apart: entry k *= s[k] (real)
+__global__ void k_scale_lines(void* tab, int fmt, const double* sv, int n, long long stride) {
+  const long long t = blockIdx.y;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const double2 v = ld(tab, t * stride + k, fmt);
+    const double f = sv[k];
+    st(tab, t * stride + k, fmt, make_double2(v.x * f, v.y * f));
+  }
+}
+
 __global__ void k_fill(void* a, int f32, long long n, double re, double im) {
   for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
     st(a, k, f32, make_double2(re, im));
@@ -252,6 +262,10 @@ int aw_k_scale(void* a, int f32, long long n, double re, double im, const double
 int aw_k_scale_n(void* a, int f32, long long n, int ninst, double re, double im, const double* ptr, void* s) {
   const int gx = (grid_for(n) + ninst - 1) / ninst;
   k_scale<<<dim3(gx, ninst), 256, 0, (cudaStream_t)s>>>(a, f32, n, re, im, ptr);
+  return ok();
+}
+int aw_k_scale_lines(void* tab, int fmt, const double* sv, int n, int count, long long stride, void* s) {
+  k_scale_lines<<<dim3((n + 255) / 256, count), 256, 0, (cudaStream_t)s>>>(tab, fmt, sv, n, stride);
   return ok();
 }
 int aw_k_fill(void* a, int f32, long long n, double re, double im, void* s) {

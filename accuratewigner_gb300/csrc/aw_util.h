@@ -9,6 +9,8 @@ extern "C" {
 int aw_k_scale(void* a, int f32, long long n, double re, double im, const double* ptr, void* s);
 // ninst instances of n elements, instance k scaled by ptr[2k..2k+1] (when ptr)
 int aw_k_scale_n(void* a, int f32, long long n, int ninst, double re, double im, const double* ptr, void* s);
+/* count tables of n complex entries, stride entries apart, each entry k times the real s[k] */
+int aw_k_scale_lines(void* tab, int fmt, const double* s, int n, int count, long long stride, void* st);
 int aw_k_fill(void* a, int f32, long long n, double re, double im, void* s);
 int aw_k_convert(const void* src, int sf32, void* dst, int df32, long long n, void* s);
 int aw_k_partial(const void* a, int f32, long long n, int mode, long long stride, double2* part, int nblocks, void* s);

@@ -111,6 +111,30 @@ def test_time_dependent_absorbers_in_both_frames():
     g.close()
 
 
+@pytest.mark.parametrize("absorber", [
+    # a product f(XX) g(XX'): folded into the kick tables
+    "exp(-dt * 0.02 * (pow(XX / XX_max, 8) + pow(XX_prime / XX_prime_max, 8)))",
+    # not a product: read per point from the 2-D mask
+    "exp(-dt * 0.02 * pow((XX - XX_prime) / XX_max, 2))",
+])
+def test_time_independent_absorbers_separable_or_not(absorber):
+    from accuratewigner_gb300 import WignerMoyalCUDA1D
+    from oracle.propagators import WignerMoyalOracle
+
+    p = dict(WM_STRONG_FIELD, abs_boundary_x=absorber)
+    g = WignerMoyalCUDA1D(**p)
+    c = WignerMoyalOracle(**p, py_functions={"E": e_field})
+    init = "exp(-pow(X - 2., 2) - P * P) / M_PI"
+    g.set_wignerfunction(init)
+    c.set_wignerfunction(init)
+    g.propagate(12)
+    c.propagate(12)
+    assert rel_l2(g.wignerfunction.get(), c.wignerfunction) < TOL
+    for name in ("X_average", "P_average", "hamiltonian_average"):
+        assert obs_close(getattr(g, name), getattr(c, name), TOL), name
+    g.close()
+
+
 def test_wigner_bloch_gibbs_matches_oracle_and_analytic():
     from accuratewigner_gb300 import WignerBlochCUDA1D
     from oracle.propagators import WignerBlochOracle
