@@ -155,11 +155,13 @@ __device__ __forceinline__ double block_sum(double x, double* red, int tid) {
   }
 }
 
-template <typename V, class Tile, int NT>
 // Register budget: 5 blocks of 128 threads (96 registers a thread) or 2 blocks of 256 per SM, and 4
 // blocks of 256 (64 registers) for 4 elements a thread.  The double-float passes are latency-bound
 // and the occupancy gained beats the few spills (measured on the 1024-point passes: 4 blocks of 128
 // threads 0.180 ms a step, 5 blocks 0.174, 6 blocks 0.183).
+// REDUCE_ONLY: the reduction-only column pass (load, FFT d1, f1, column reductions, nothing stored),
+// compiled without the segment loop so that its code is a fraction of the full pass's.
+template <typename V, class Tile, int NT, bool REDUCE_ONLY = false>
 __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 1)
                                                               : (NT <= 128 ? 5 : (NT <= 256 ? 2 : 1))))
     aw_pass_kernel(const __grid_constant__ AwPassArgs a) {
@@ -187,6 +189,10 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
 #pragma unroll
   for (int k = 0; k < E; ++k) r[k] = in[gidx<Tile>(lg, pos0 + k * STEP, ncols)];
 
+  if constexpr (REDUCE_ONLY) {
+    run_fft<Tile, NT>(r, s, tw, a.d1, tid);
+    if (a.f1.active) apply_factor<V, Tile, NT>(r, a.f1, lg, pos0, a.nrows, ncols, toff, eoff, inst);
+  } else {
   // The pass as a loop over FFT segments, so that the kernel holds one copy of the FFT and of
   // the factor code:
   //   0: f0, FFT d1, f1        then mid_out, diag_out, red_abs2 (start)
@@ -236,6 +242,7 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
     for (int k = 0; k < E; ++k) acc += cabs2(r[k]);
     const double tot = block_sum<NT>(to_d(acc), red, tid);
     if (tid == 0) a.red_abs2[(long long)inst * gridDim.x + blockIdx.x] = tot;
+  }
   }
 
   if constexpr (!Tile::IS_ROW) {
@@ -421,9 +428,14 @@ static int launch_col_t(const AwPassArgs* a, int batch, cudaStream_t st) {
     const bool clustered = a->alt_cross && a->cluster > 1;
     // a clustered launch keeps one row of partials (N complex FP64) behind the tile
     const size_t smem = sizeof(V) * Tile::SMEM_ELEMS + (clustered ? sizeof(double2) * N : 0);
-    auto kern = aw_pass_kernel<V, Tile, S::NT>;
-    static int max_dyn = prepare_smem(kern, sizeof(V) * Tile::SMEM_ELEMS + sizeof(double2) * N);
-    if (max_dyn < (int)smem) return -3;
+    const bool reduce_only = !a->out && !a->mid_out && !a->br_out && !a->f0.active && !a->d2 && !a->f2.active &&
+                             !a->f3.active && !a->red_abs2 && (a->col_alt || a->alt_cross || a->red_line);
+    auto kern = reduce_only ? aw_pass_kernel<V, Tile, S::NT, true> : aw_pass_kernel<V, Tile, S::NT, false>;
+    static int max_dyn = prepare_smem(aw_pass_kernel<V, Tile, S::NT, false>,
+                                      sizeof(V) * Tile::SMEM_ELEMS + sizeof(double2) * N);
+    static int max_dyn_r = prepare_smem(aw_pass_kernel<V, Tile, S::NT, true>,
+                                        sizeof(V) * Tile::SMEM_ELEMS + sizeof(double2) * N);
+    if ((reduce_only ? max_dyn_r : max_dyn) < (int)smem) return -3;
     dim3 grid(a->ncols / LINES, batch);
     if (!clustered) {
       kern<<<grid, S::NT, smem, st>>>(*a);
