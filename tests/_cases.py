@@ -32,3 +32,14 @@ WM_STRONG_FIELD = dict(
     diff_K="P", diff_V="X / pow(X * X + 2., 1.5) + E(t)",
     abs_boundary_x="pow(abs(sin(0.5 * M_PI * (XX + XX_max) / XX_max) * sin(0.5 * M_PI * (XX_prime + XX_prime_max) / XX_prime_max)), dt * 0.05)",
 )
+
+# von Neumann: anharmonic oscillator, a displaced boosted Gaussian pure state
+VN = dict(t=0.0, dt=0.005, X_gridDIM=128, X_amplitude=10.0, omega_square=0.05, sigma=1.0, p0=0.5, x0=0.5,
+          K="0.5 * P * P", V="0.5 * omega_square * X * X + 0.01 * X * X * X * X",
+          diff_K="P", diff_V="omega_square * X + 0.04 * X * X * X")
+VN_INIT = ("exp(-sigma * pow(X - x0, 2) + cuda_complex(0., p0) * X) * "
+           "exp(-sigma * pow(X_prime - x0, 2) - cuda_complex(0., p0) * X_prime)")
+
+# Schrodinger: anharmonic oscillator
+SW = dict(t=0.0, dt=0.01, X_gridDIM=256, X_amplitude=10.0, K="0.5 * P * P", V="0.5 * X * X + 0.05 * X * X * X * X",
+          diff_K="P", diff_V="X + 0.2 * X * X * X")

@@ -3,16 +3,12 @@ import numpy as np
 import pytest
 
 from conftest import obs_close, rel_l2
+from _cases import SW, VN, VN_INIT
 
 pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("c128_engine")]
 
 TOL = 1e-10
 
-VN = dict(t=0.0, dt=0.005, X_gridDIM=128, X_amplitude=10.0, omega_square=0.05, sigma=1.0, p0=0.5, x0=0.5,
-          K="0.5 * P * P", V="0.5 * omega_square * X * X + 0.01 * X * X * X * X",
-          diff_K="P", diff_V="omega_square * X + 0.04 * X * X * X")
-VN_INIT = ("exp(-sigma * pow(X - x0, 2) + cuda_complex(0., p0) * X) * "
-           "exp(-sigma * pow(X_prime - x0, 2) - cuda_complex(0., p0) * X_prime)")
 
 
 def test_von_neumann_propagate_ehrenfest():
@@ -84,8 +80,6 @@ def test_rho_bloch_ground_state():
     assert rel_l2(g.rho.get(), c.rho) < 1e-8
 
 
-SW = dict(t=0.0, dt=0.01, X_gridDIM=256, X_amplitude=10.0, K="0.5 * P * P", V="0.5 * X * X + 0.05 * X * X * X * X",
-          diff_K="P", diff_V="X + 0.2 * X * X * X")
 
 
 def test_schrodinger_propagate_ehrenfest_and_wigner():

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from conftest import obs_close, rel_l2
-from _cases import WM_ANHARMONIC, WM_INIT, WM_STRONG_FIELD, e_field
+from _cases import SW, VN, VN_INIT, WM_ANHARMONIC, WM_INIT, WM_STRONG_FIELD, e_field
 
 pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("c128_engine")]
 
@@ -46,7 +46,6 @@ def test_wigner_moyal_single_steps(case):
 def test_von_neumann_single_steps():
     from accuratewigner_gb300 import RhoVNeumannCUDA1D
     from oracle.propagators import RhoVNeumannOracle
-    from test_rho_schrodinger_gpu import VN, VN_INIT
 
     g = RhoVNeumannCUDA1D(**VN)
     c = RhoVNeumannOracle(**VN)
@@ -61,7 +60,6 @@ def test_von_neumann_single_steps():
 def test_schrodinger_single_steps_and_get_ehrenfest():
     from accuratewigner_gb300 import SchrodingerWignerCUDA1D
     from oracle.propagators import SchrodingerWignerOracle
-    from test_rho_schrodinger_gpu import SW
 
     g = SchrodingerWignerCUDA1D(**SW)
     c = SchrodingerWignerOracle(**SW)
