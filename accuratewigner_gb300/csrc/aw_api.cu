@@ -1665,17 +1665,21 @@ static int prepare_maskx(aw_state_s* h) {
   if (h->ni != 1) return AW_OK;
   const int nr = h->nr, nc = h->nc;
   const size_t n = (size_t)nr * nc;
+  // read back on the handle's stream (non-blocking: a plain cudaMemcpy would not wait for the build)
   std::vector<double> m(n);
   if (h->f32) {
     std::vector<float> f(n);
-    CK(cudaMemcpy(f.data(), h->maskx.p, n * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(f.data(), h->maskx.p, n * 4, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
     for (size_t k = 0; k < n; ++k) m[k] = f[k];
   } else if (h->df) {
     std::vector<float> f(2 * n);
-    CK(cudaMemcpy(f.data(), h->maskx.p, n * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(f.data(), h->maskx.p, n * 8, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
     for (size_t k = 0; k < n; ++k) m[k] = (double)f[2 * k] + (double)f[2 * k + 1];
   } else {
-    CK(cudaMemcpy(m.data(), h->maskx.p, n * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(m.data(), h->maskx.p, n * 8, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
   }
   size_t piv = 0;
   for (size_t k = 1; k < n; ++k)
@@ -1693,7 +1697,8 @@ static int prepare_maskx(aw_state_s* h) {
   for (int j = 0; j < nc; ++j) sv[j] = m[(size_t)i0 * nc + j];
   for (int i = 0; i < nr; ++i) sv[nc + i] = m[(size_t)i * nc + j0] / m[piv];
   TRY(dalloc(h->masksep, sv.size() * sizeof(double)));
-  CK(cudaMemcpy(h->masksep.p, sv.data(), sv.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(h->masksep.p, sv.data(), sv.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
   h->maskx_sep = true;
   return AW_OK;
 }
