@@ -345,16 +345,24 @@ static double define_round(double v) {
 // (re hi, im hi, re lo, im lo)).
 static int tab_fmt(const aw_state_s* h) { return h->f32 ? 1 : (h->df ? 2 : 0); }
 
+// Host-to-device copy that has landed when it returns: a pageable cudaMemcpy may return before its
+// DMA completes, and the handle's non-blocking streams do not wait for the legacy stream.
+static int h2d(void* dst, const void* src, size_t bytes) {
+  CK(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+  CK(cudaStreamSynchronize(cudaStreamLegacy));
+  return AW_OK;
+}
+
 // upload a complex table (interleaved re, im) in table format fmt
 static int upload_reals(DevBuf& dst, const std::vector<double>& v, int fmt) {
   const size_t n = v.size();
   TRY(dalloc(dst, n * (fmt == 1 ? 4 : 8)));
   if (n == 0) return AW_OK;
   if (fmt == 0) {
-    CK(cudaMemcpy(dst.p, v.data(), n * 8, cudaMemcpyHostToDevice));
+    TRY(h2d(dst.p, v.data(), n * 8));
   } else if (fmt == 1) {
     std::vector<float> g(v.begin(), v.end());
-    CK(cudaMemcpy(dst.p, g.data(), n * 4, cudaMemcpyHostToDevice));
+    TRY(h2d(dst.p, g.data(), n * 4));
   } else {
     // complex entries (re, im) as (re hi, im hi, re lo, im lo)
     std::vector<float> g(2 * n);
@@ -365,7 +373,7 @@ static int upload_reals(DevBuf& dst, const std::vector<double>& v, int fmt) {
       g[2 * k + 2] = (float)(v[k] - (double)rh);
       g[2 * k + 3] = (float)(v[k + 1] - (double)ih);
     }
-    CK(cudaMemcpy(dst.p, g.data(), n * 8, cudaMemcpyHostToDevice));
+    TRY(h2d(dst.p, g.data(), n * 8));
   }
   return AW_OK;
 }
@@ -929,20 +937,20 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
   TRY(dalloc(h->rho, ni * grid * h->esz));
   TRY(dalloc(h->W, ni * wgrid * h->esz));
   TRY(dalloc(h->tmp, std::max(ni * grid, wgrid) * 16));
-  CK(cudaMemset(h->rho.p, 0, ni * grid * h->esz));
-  CK(cudaMemset(h->W.p, 0, ni * wgrid * h->esz));
+  CK(cudaMemsetAsync(h->rho.p, 0, ni * grid * h->esz, h->st));
+  CK(cudaMemsetAsync(h->W.p, 0, ni * wgrid * h->esz, h->st));
   TRY(dalloc(h->tabs, ni * TAB_NSLOT * (h->nc + h->nr) * h->esz));
   const size_t nscal = 2 * ni + 16 + ni * FIN_TV;
   TRY(dalloc(h->scal, nscal * sizeof(double)));
   TRY(dalloc(h->stop, 2 * ni * sizeof(int)));
   TRY(dalloc(h->part, 1024 * sizeof(double2)));
-  CK(cudaMemset(h->scal.p, 0, nscal * sizeof(double)));
-  CK(cudaMemset(h->stop.p, 0, 2 * ni * sizeof(int)));
+  CK(cudaMemsetAsync(h->scal.p, 0, nscal * sizeof(double), h->st));
+  CK(cudaMemsetAsync(h->stop.p, 0, 2 * ni * sizeof(int), h->st));
   TRY(dalloc(h->bvec, 4 * ni * sizeof(double)));
-  CK(cudaMemset(h->bvec.p, 0, 4 * ni * sizeof(double)));
+  CK(cudaMemsetAsync(h->bvec.p, 0, 4 * ni * sizeof(double), h->st));
   if (h->np) {
     TRY(dalloc(h->params, ni * h->np * sizeof(double)));
-    CK(cudaMemset(h->params.p, 0, ni * h->np * sizeof(double)));
+    CK(cudaMemsetAsync(h->params.p, 0, ni * h->np * sizeof(double), h->st));
   }
   {
     // term tables: int slot[64], kind[64], idx[64], double coef[64]
@@ -955,8 +963,8 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
       ti[128 + k] = h->tidx[k];
       tc[k] = h->tcoef[k];
     }
-    CK(cudaMemcpy(h->terms.p, ti.data(), ti.size() * sizeof(int), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy((char*)h->terms.p + 64 * 3 * sizeof(int), tc.data(), tc.size() * 8, cudaMemcpyHostToDevice));
+    TRY(h2d(h->terms.p, ti.data(), ti.size() * sizeof(int)));
+    TRY(h2d((char*)h->terms.p + 64 * 3 * sizeof(int), tc.data(), tc.size() * 8));
   }
 
   // twiddles
@@ -1149,7 +1157,7 @@ static int clear_stops(aw_state_s* h);
 static int ensure_snap(aw_state_s* h) {
   if (h->snap.p) return AW_OK;
   TRY(dalloc(h->snap, (size_t)h->ni * gsz(h) * h->esz));
-  CK(cudaMemset(h->snap.p, 0, (size_t)h->ni * gsz(h) * h->esz));
+  CK(cudaMemsetAsync(h->snap.p, 0, (size_t)h->ni * gsz(h) * h->esz, h->st));
   return AW_OK;
 }
 
