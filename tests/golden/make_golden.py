@@ -2,7 +2,8 @@
 
 Runs only where the reference checkout exists (the build container):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # the cases that have no file yet
+    python tests/golden/make_golden.py --all    # every case
 
 Each case runs a small configuration through oracle/ref_kernels.py, i.e. the
 reference's CUDA-C kernels compiled for the CPU by oracle/ref_build.py, driven
@@ -49,9 +50,15 @@ def run_case(name, spec):
             out["K_min"] = obj.K_min
         elif verb == "ground":
             obj.set_ground_state(arg)
+        elif verb == "single_steps":
+            for _ in range(arg):
+                obj.t += obj.dt
+                obj.single_step_propagation()
         elif verb == "save":
             what = arg
-            if what == "wigner":
+            if what == "rho_single":
+                out["rho_single"] = np.array(obj.rho)
+            elif what == "wigner":
                 out["wigner"] = np.array(obj.wignerfunction)
             elif what == "rho":
                 out["rho"] = np.array(obj.rho)
@@ -82,7 +89,10 @@ def run_case(name, spec):
 def main():
     if not ref_build.available():
         sys.exit("the reference checkout is needed to regenerate the golden vectors")
+    redo = "--all" in sys.argv
     for name, spec in CASES.items():
+        if not redo and os.path.exists(os.path.join(HERE, name + ".npz")):
+            continue
         out = run_case(name, spec)
         meta = json.dumps({"kind": spec["kind"], "ops": spec["ops"]})
         np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=np.array(meta), **out)

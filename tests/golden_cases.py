@@ -58,6 +58,26 @@ CASES = {
         ops=[["set_psi", "exp(-pow(X - 1., 2) + cuda_complex(0., 0.5) * X)"], ["propagate", 15], ["save", "psi"],
              ["save", "ehrenfest"], ["save", "sw_wigner"], ["ground", 200], ["save", "energy"]],
     ),
+    # Wigner-Moyal with absorbing boundaries that depend on t in both frames and a driven potential,
+    # Ehrenfest every step, then single steps (wm:543-561) at the advanced times
+    "wm_tdep_absorbers": dict(
+        kind="wm",
+        params=dict(t=0.1, dt=0.02, X_gridDIM=64, X_amplitude=8.0, P_gridDIM=32, P_amplitude=5.0, F=0.3,
+                    K="0.5 * P * P", V="0.5 * X * X + X * F * sin(0.7 * t)", diff_K="P", diff_V="X + F * sin(0.7 * t)",
+                    abs_boundary_x="pow(abs(cos(0.5 * M_PI * XX / (XX_max + dXX)) * cos(0.5 * M_PI * XX_prime / (XX_prime_max + dXX_prime))), dt * (0.1 + 0.05 * sin(t)))",
+                    abs_boundary_p="exp(-0.001 * dt * (1. + cos(0.5 * t)) * (PP * PP + PP_prime * PP_prime))"),
+        ops=[["set_wigner", "exp(-pow(X + 0.5, 2) - pow(P - 0.3, 2))"], ["propagate", 8], ["save", "wigner"],
+             ["save", "rho"], ["save", "ehrenfest"], ["single_steps", 2], ["save", "rho_single"]],
+    ),
+    # von Neumann single steps (vn:450-468): not normalised
+    "vn_single_steps": dict(
+        kind="vn",
+        params=dict(t=0.0, dt=0.01, X_gridDIM=64, X_amplitude=8.0, sigma=1.0, p0=0.4, x0=0.5,
+                    K="0.5 * P * P", V="0.1 * X * X + 0.01 * X * X * X * X"),
+        ops=[["set_rho", "exp(-sigma * pow(X - x0, 2) + cuda_complex(0., p0) * X) * "
+                         "exp(-sigma * pow(X_prime - x0, 2) - cuda_complex(0., p0) * X_prime)"],
+             ["single_steps", 3], ["save", "rho_single"]],
+    ),
 }
 
 
@@ -89,8 +109,14 @@ def run_ops(obj, spec):
             out["K_min"] = obj.K_min
         elif verb == "ground":
             obj.set_ground_state(arg)
+        elif verb == "single_steps":
+            for _ in range(arg):
+                obj.t += obj.dt
+                obj.single_step_propagation()
         elif verb == "save":
-            if arg == "wigner":
+            if arg == "rho_single":
+                out["rho_single"] = _arr(obj.rho)
+            elif arg == "wigner":
                 out["wigner"] = _arr(obj.wignerfunction)
             elif arg == "rho":
                 out["rho"] = _arr(obj.rho)
