@@ -33,6 +33,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -91,12 +92,14 @@ def _rank():
 
 
 class ClockSampler:
-    """nvidia-smi samples during the timed region."""
+    """nvidia-smi samples during the timed region, kept as a CSV in $AW_CLOCKS_DIR (default: the
+    temporary directory)."""
 
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+        self.path = os.path.join(os.environ.get("AW_CLOCKS_DIR") or tempfile.gettempdir(),
+                                 "clocks_bench_%d.csv" % os.getpid())
 
     def __enter__(self):
         try:
@@ -557,7 +560,6 @@ def run_frames(args):
     """The headline run with its on-disk record: a frame (W, t, diagonal of rho) saved every 100 steps
     through the asynchronous writer, against the same steps without frames."""
     import shutil
-    import tempfile
 
     import torch
 
