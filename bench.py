@@ -275,7 +275,7 @@ def run_ours(args):
             "scaling": "weak",
             "vs_baseline": None,
             "dtype": DTYPE[args.precision],
-            "data": "synthetic (config 2 shapes; Gibbs-state initial condition)",
+            "data": "synthetic (the 1024x1024 strong-field shapes; Gibbs-state initial condition)",
             "config": {
                 "workload": "strong-field Wigner-Moyal, 1024x1024 (x,p), X_amplitude=60, P_amplitude=6, soft-core V + "
                             "x E(t), dt=0.05, cos^(1/8) absorber, Ehrenfest every step",
@@ -368,7 +368,7 @@ def run_reference(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic (config 2 shapes)",
+        "data": "synthetic (the 1024x1024 strong-field shapes)",
         "config": {"workload": "strong-field Wigner-Moyal, 1024x1024 (x,p), X_amplitude=60, P_amplitude=6, soft-core V "
                                "+ x E(t), dt=0.05, cos^(1/8) absorber, Ehrenfest every step",
                    "precision": "c128", "grid": [N_GRID, N_GRID]},

@@ -23,7 +23,7 @@ __device__ double E(double t)
 }
 """
 
-# time-dependent strong-field form with an absorbing boundary (the config 2 recipe, small grid)
+# time-dependent strong-field form with an absorbing boundary (the 1024^2 strong-field recipe on a small grid)
 WM_STRONG_FIELD = dict(
     t=0.0, dt=0.05, X_gridDIM=128, X_amplitude=30.0, P_gridDIM=128, P_amplitude=4.0,
     E0=0.04, omega=0.057, ncyc=5,
