@@ -45,8 +45,8 @@ CLASSES = {"wm": WignerMoyalCUDA1D, "vn": RhoVNeumannCUDA1D, "rb": RhoBlochCUDA1
 
 # Relative L2 error of a complex64 propagation after `steps` steps on an n x n grid, against the FP64
 # result: the FP32 rounding of each FFT stage of the 4 propagation transforms a step adds up like a
-# random walk, err = C eps32 sqrt(4 steps log2 n).  C = 3 bounds the measured values (anharmonic Wigner-Moyal 256^2,
-# 1000 steps: 1.4e-5, C = 1.3; strong-field 1024^2, 1000 steps: 3.2e-5, C = 2.7).
+# random walk, err = C eps32 sqrt(4 steps log2 n).  C = 3 bounds the measured values (anharmonic
+# Wigner-Moyal 256^2, 1000 steps: 1.4e-5, C = 1.3; strong-field 1024^2, 1000 steps: 3.2e-5, C = 2.7).
 C64_ERROR_C = 3.0
 EPS32 = 2.0 ** -24
 

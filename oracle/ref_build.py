@@ -1,9 +1,10 @@
 """Compile the reference's own CUDA-C kernel templates for the CPU.
 
 TEST INFRASTRUCTURE ONLY: used to generate the golden vectors under
-``tests/golden/`` (tests/golden/make_golden.py).  Nothing in the library,
-the GPU tests, smoke() or bench.py runs it, and it needs the reference
-checkout, which exists only in the build container.
+``tests/golden/`` (tests/golden/make_golden.py).  ``__graft_entry__.build()``
+compiles the modules of the golden configurations where the reference checkout
+exists (the build container only); nothing in the library, the GPU tests,
+smoke() or bench.py runs them.
 
 The reference keeps its kernels as CUDA-C strings inside Python 2 classes
 (e.g. wigner_moyal_cuda_1d.py:624-828) and formats them with str.format
