@@ -318,8 +318,8 @@ extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw
 //   P-marginal  r_i = Sum_j Re W_ij = (-1)^i Np Re w_{(-i) mod Np},  w_m = Sum_j (-1)^j Q_j(m)
 //   purity      2 pi dXdP Sum Re W^2 / norm^2 = 2 pi dXdP Np Sum |rho|^2 / norm^2 (the transform is
 //               unitary up to the factor Np of the unnormalised ifft0)
-// One block per term, one for the norm, one for Sum |rho|^2; the last block to finish combines
-// them in a fixed order.
+// Blocks per term, for the norm and for Sum |rho|^2, each over a chunk of columns or rows; the last
+// block to finish combines them in a fixed order.
 extern "C" __global__ void aw_finalize_rot(const double2* aw_z, const double2* aw_wpart, int aw_nparts,
                                            const double* aw_abs2, int aw_nb2, double* aw_tv, unsigned int* aw_counter,
                                            double* aw_hist, double* aw_inv_norm, int* aw_stop, int aw_stop_on_purity,
@@ -330,6 +330,8 @@ extern "C" __global__ void aw_finalize_rot(const double2* aw_z, const double2* a
   // blocks: (term or norm or purity) x chunk; FP64 expression evaluation spread over the GPU.
   // blockIdx.y = instance of a batch, with its own marginals, partials, history row and scalars.
   __shared__ double aw_red[256];
+  __shared__ double aw_wg[256];
+  __shared__ double aw_fsum[66];
   __shared__ int aw_is_last;
   {
     const long long aw_in = blockIdx.y;
@@ -359,22 +361,34 @@ extern "C" __global__ void aw_finalize_rot(const double2* aw_z, const double2* a
         aw_s += aw_cj * aw_obs_x(aw_idx, X, t, aw_prm);
       }
     } else {
+      // aw_gs threads share each row's partials (every aw_gs-th one, in four interleaved sums so that
+      // their loads are in flight together); the group sums meet in shared memory and add in a fixed
+      // order.  Row counts and the block size are powers of two, so every sweep fills the block.
       const int aw_len = aw_nrow / aw_nchunk, aw_lo = aw_c * aw_len;
-      for (int aw_i = aw_lo + aw_t; aw_i < aw_lo + aw_len; aw_i += aw_nt) {
-        const double P = aw_dP * ((aw_size_t)aw_i - 0.5 * aw_nrow);
+      const int aw_gs = aw_len < aw_nt ? aw_nt / aw_len : 1;
+      const int aw_rows = aw_nt / aw_gs;
+      const int aw_r = aw_t % aw_rows, aw_g = aw_t / aw_rows;
+      for (int aw_i0 = aw_lo; aw_i0 < aw_lo + aw_len; aw_i0 += aw_rows) {
+        const int aw_i = aw_i0 + aw_r;
         const int aw_k = (aw_nrow - aw_i) & (aw_nrow - 1);
-        // the partials of w_k in four interleaved sums (loads in flight together), added in a fixed order
         double aw_w0 = 0.0, aw_w1 = 0.0, aw_w2 = 0.0, aw_w3 = 0.0;
-        int aw_p = 0;
-        for (; aw_p + 4 <= aw_nparts; aw_p += 4) {
+        int aw_p = aw_g;
+        for (; aw_p + 3 * aw_gs < aw_nparts; aw_p += 4 * aw_gs) {
           aw_w0 += aw_wpart[(long long)aw_p * aw_nrow + aw_k].x;
-          aw_w1 += aw_wpart[(long long)(aw_p + 1) * aw_nrow + aw_k].x;
-          aw_w2 += aw_wpart[(long long)(aw_p + 2) * aw_nrow + aw_k].x;
-          aw_w3 += aw_wpart[(long long)(aw_p + 3) * aw_nrow + aw_k].x;
+          aw_w1 += aw_wpart[(long long)(aw_p + aw_gs) * aw_nrow + aw_k].x;
+          aw_w2 += aw_wpart[(long long)(aw_p + 2 * aw_gs) * aw_nrow + aw_k].x;
+          aw_w3 += aw_wpart[(long long)(aw_p + 3 * aw_gs) * aw_nrow + aw_k].x;
         }
-        for (; aw_p < aw_nparts; ++aw_p) aw_w0 += aw_wpart[(long long)aw_p * aw_nrow + aw_k].x;
-        const double aw_w = (aw_w0 + aw_w1) + (aw_w2 + aw_w3);
-        aw_s += ((aw_i & 1) ? -1.0 : 1.0) * aw_nrow * aw_w * aw_obs_p(aw_idx, P, t, aw_prm);
+        for (; aw_p < aw_nparts; aw_p += aw_gs) aw_w0 += aw_wpart[(long long)aw_p * aw_nrow + aw_k].x;
+        aw_wg[aw_t] = (aw_w0 + aw_w1) + (aw_w2 + aw_w3);
+        __syncthreads();
+        if (aw_g == 0) {
+          double aw_w = aw_wg[aw_r];
+          for (int aw_q2 = 1; aw_q2 < aw_gs; ++aw_q2) aw_w += aw_wg[aw_q2 * aw_rows + aw_r];
+          const double P = aw_dP * ((aw_size_t)aw_i - 0.5 * aw_nrow);
+          aw_s += ((aw_i & 1) ? -1.0 : 1.0) * aw_nrow * aw_w * aw_obs_p(aw_idx, P, t, aw_prm);
+        }
+        __syncthreads();
       }
     }
   } else if (aw_q == aw_nterms) {
@@ -392,26 +406,32 @@ extern "C" __global__ void aw_finalize_rot(const double2* aw_z, const double2* a
     aw_is_last = aw_prev == gridDim.x - 1;
   }
   __syncthreads();
-  if (aw_is_last && aw_t == 0) {
+  if (aw_is_last) {
     __threadfence();
+    // one warp per term (or norm, or purity): lane sums over the chunks, then a shuffle tree
     const volatile double* aw_vt = aw_tv;
-    double aw_sum[66];
-    for (int aw_k = 0; aw_k < aw_nterms + 2; ++aw_k) {
+    const int aw_lane = aw_t & 31;
+    for (int aw_k = aw_t >> 5; aw_k < aw_nterms + 2; aw_k += aw_nt >> 5) {
       double aw_acc = 0.0;
-      for (int aw_cc = 0; aw_cc < aw_nchunk; ++aw_cc) aw_acc += aw_vt[aw_k * aw_nchunk + aw_cc];
-      aw_sum[aw_k] = aw_acc;
+      for (int aw_cc = aw_lane; aw_cc < aw_nchunk; aw_cc += 32) aw_acc += aw_vt[aw_k * aw_nchunk + aw_cc];
+      for (int aw_o = 16; aw_o > 0; aw_o >>= 1) aw_acc += __shfl_down_sync(0xffffffffu, aw_acc, aw_o);
+      if (aw_lane == 0) aw_fsum[aw_k] = aw_acc;
     }
-    const double aw_norm = aw_sum[aw_nterms] * aw_dXdP;
-    for (int aw_k = 0; aw_k < aw_nslots; ++aw_k) aw_hist[aw_k] = 0.0;
-    for (int aw_k = 0; aw_k < aw_nterms; ++aw_k)
-      aw_hist[aw_tslot[aw_k]] += aw_tcoef[aw_k] * (aw_sum[aw_k] * aw_dXdP / aw_norm);
-    const double aw_purity = 2.0 * M_PI * aw_dXdP * aw_nrow * aw_sum[aw_nterms + 1] / (aw_norm * aw_norm);
-    aw_hist[aw_nslots] = aw_purity;
-    aw_hist[aw_nslots + 1] = aw_norm;
-    aw_inv_norm[0] = 1.0 / aw_norm;
-    aw_inv_norm[1] = 0.0;
-    if (aw_stop && aw_stop_on_purity && !(aw_purity < 1.0)) *aw_stop = 1;
-    *aw_counter = 0u;
+    __syncthreads();
+    if (aw_t == 0) {
+      const double* aw_sum = aw_fsum;
+      const double aw_norm = aw_sum[aw_nterms] * aw_dXdP;
+      for (int aw_k = 0; aw_k < aw_nslots; ++aw_k) aw_hist[aw_k] = 0.0;
+      for (int aw_k = 0; aw_k < aw_nterms; ++aw_k)
+        aw_hist[aw_tslot[aw_k]] += aw_tcoef[aw_k] * (aw_sum[aw_k] * aw_dXdP / aw_norm);
+      const double aw_purity = 2.0 * M_PI * aw_dXdP * aw_nrow * aw_sum[aw_nterms + 1] / (aw_norm * aw_norm);
+      aw_hist[aw_nslots] = aw_purity;
+      aw_hist[aw_nslots + 1] = aw_norm;
+      aw_inv_norm[0] = 1.0 / aw_norm;
+      aw_inv_norm[1] = 0.0;
+      if (aw_stop && aw_stop_on_purity && !(aw_purity < 1.0)) *aw_stop = 1;
+      *aw_counter = 0u;
+    }
   }
 }
 
