@@ -1519,8 +1519,9 @@ static int launch_finalize_rot(aw_state_s* h, double t, double* hist_row, int st
   const double* tc = (const double*)((const char*)h->terms.p + 64 * 3 * sizeof(int));
   int nterms = (int)h->tslot.size(), nslots = h->cfg.n_slots;
   // chunks per term: enough blocks to spread the FP64 expression work and the loads of the row
-  // partials over the SMs
-  int nchunk = 64;
+  // partials over the SMs, at least 16 columns or rows each (smaller chunks slow small grids, whose
+  // steps wait for this reduction)
+  int nchunk = std::max(1, std::min(64, std::min(ncol, nrow) / 16));
   while (nchunk > 1 && ((std::min(ncol, nrow) % nchunk) || (nterms + 2) * nchunk > 1024)) nchunk >>= 1;
   void* args[] = {&z, &wpart, &nparts, &abs2, &nb2, &tv, &counter, &hist_row, &inv, &stop, &stop_on_purity, &t,
                   &ncol, &nrow, &dX, &dP, &dXdP, &ts, &tk, &ti, &tc, &nterms, &nslots, &nchunk, &prm, &np, &hstride};
