@@ -11,5 +11,7 @@ from .wigner_bloch_cuda_1d import WignerBlochCUDA1D
 from .rho_vneumann_cuda_1d import RhoVNeumannCUDA1D
 from .rho_bloch_cuda_1d import RhoBlochCUDA1D
 from .schrodinger_wigner_cuda_1d import SchrodingerWignerCUDA1D
+from ._common import check_config
 
-__all__ = ["WignerMoyalCUDA1D", "WignerBlochCUDA1D", "RhoVNeumannCUDA1D", "RhoBlochCUDA1D", "SchrodingerWignerCUDA1D"]
+__all__ = ["WignerMoyalCUDA1D", "WignerBlochCUDA1D", "RhoVNeumannCUDA1D", "RhoBlochCUDA1D", "SchrodingerWignerCUDA1D",
+           "check_config"]

@@ -6,6 +6,7 @@ rho_vneumann_cuda_1d.py:48-179, schrodinger_wigner_cuda_1d.py:50-151).
 """
 import ctypes
 import re
+import threading
 import types
 
 import numpy as np
@@ -207,11 +208,38 @@ def apply_batch(cfg, kwargs, keep):
     cfg.init_expr = b
 
 
+class _ConfigChecked(Exception):
+    """Ends a constructor run by check_config once its configuration has been checked."""
+
+
+_CHECK = threading.local()
+
+
+def check_config(cls, arch="sm_103a", **kwargs):
+    """Run the constructor of a propagator class up to its native handle, then validate the
+    configuration and compile its expression strings with NVRTC for `arch` instead of creating the
+    handle: no GPU is needed.  Raises what the constructor would raise (AttributeError for a
+    missing keyword, AssertionError for a grid that is not a power of two, RuntimeError for an
+    expression that does not compile); returns None when the configuration is good."""
+    _CHECK.arch = arch
+    try:
+        cls(**kwargs)
+    except _ConfigChecked:
+        return None
+    finally:
+        _CHECK.arch = None
+    raise RuntimeError("%s made no native handle" % cls.__name__)
+
+
 class Handle:
     """Owns one native propagator handle."""
 
     def __init__(self, cfg):
         lib = _lib.load()
+        arch = getattr(_CHECK, "arch", None)
+        if arch is not None:
+            _lib.check(lib.aw_check_config(ctypes.byref(cfg), arch.encode()))
+            raise _ConfigChecked()
         h = ctypes.c_void_p()
         _lib.check(lib.aw_create(ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h

@@ -95,6 +95,7 @@ SIGNATURES = [
     ("aw_profile_read", c_int, [c_vp, ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl), ctypes.POINTER(c_i64)]),
     ("aw_create", c_int, [ctypes.POINTER(AwConfig), ctypes.POINTER(c_vp)]),
     ("aw_destroy", c_int, [c_vp]),
+    ("aw_check_config", c_int, [ctypes.POINTER(AwConfig), c_cp]),
     ("aw_stream", c_int, [c_vp, ctypes.POINTER(c_vp)]),
     ("aw_sync", c_int, [c_vp]),
     ("aw_bloch_min", c_int, [c_vp, ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl)]),

@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <tuple>
@@ -69,6 +70,29 @@ struct JitLib {
 static std::mutex g_jit_mu;
 static std::unordered_map<std::string, cudaLibrary_t> g_jit_cache;
 
+// NVRTC: `src` compiled for the option `arch` ("--gpu-architecture=sm_103a"); needs no device
+static int nvrtc_cubin(const std::string& src, const char* arch, std::vector<char>* cubin) {
+  nvrtcProgram prog;
+  if (nvrtcCreateProgram(&prog, src.c_str(), "aw_user.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+    return fail(AW_E_JIT, "nvrtcCreateProgram failed");
+  const char* opts[] = {arch, "--std=c++17", "-lineinfo"};
+  nvrtcResult r = nvrtcCompileProgram(prog, 3, opts);
+  if (r != NVRTC_SUCCESS) {
+    size_t n = 0;
+    nvrtcGetProgramLogSize(prog, &n);
+    std::string log(n, '\0');
+    nvrtcGetProgramLog(prog, &log[0]);
+    nvrtcDestroyProgram(&prog);
+    return fail(AW_E_JIT, "NVRTC could not compile the user expressions:\n%s", log.c_str());
+  }
+  size_t n = 0;
+  nvrtcGetCUBINSize(prog, &n);
+  cubin->resize(n);
+  nvrtcGetCUBIN(prog, cubin->data());
+  nvrtcDestroyProgram(&prog);
+  return AW_OK;
+}
+
 static int jit_compile(const std::string& src, cudaLibrary_t* out) {
   int dev = 0, maj = 0, mnr = 0;
   CK(cudaGetDevice(&dev));
@@ -85,24 +109,8 @@ static int jit_compile(const std::string& src, cudaLibrary_t* out) {
       return AW_OK;
     }
   }
-  nvrtcProgram prog;
-  if (nvrtcCreateProgram(&prog, src.c_str(), "aw_user.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
-    return fail(AW_E_JIT, "nvrtcCreateProgram failed");
-  const char* opts[] = {arch, "--std=c++17", "-lineinfo"};
-  nvrtcResult r = nvrtcCompileProgram(prog, 3, opts);
-  if (r != NVRTC_SUCCESS) {
-    size_t n = 0;
-    nvrtcGetProgramLogSize(prog, &n);
-    std::string log(n, '\0');
-    nvrtcGetProgramLog(prog, &log[0]);
-    nvrtcDestroyProgram(&prog);
-    return fail(AW_E_JIT, "NVRTC could not compile the user expressions:\n%s", log.c_str());
-  }
-  size_t n = 0;
-  nvrtcGetCUBINSize(prog, &n);
-  std::vector<char> cubin(n);
-  nvrtcGetCUBIN(prog, cubin.data());
-  nvrtcDestroyProgram(&prog);
+  std::vector<char> cubin;
+  TRY(nvrtc_cubin(src, arch, &cubin));
   cudaLibrary_t lib;
   CK(cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
   std::lock_guard<std::mutex> lk(g_jit_mu);
@@ -819,7 +827,8 @@ static int upload_bloch(aw_state_s* h, const double* dbeta) {
   return AW_OK;
 }
 
-static int create_impl(const aw_config* cfg, aw_state_s* h) {
+// check_only: validate the configuration and stop before the first CUDA call
+static int create_impl(const aw_config* cfg, aw_state_s* h, bool check_only = false) {
   h->cfg = *cfg;
   h->kind = cfg->kind;
   if (cfg->precision < AW_C128 || cfg->precision > AW_C128_FP64) return fail(AW_E_ARG, "unknown precision %d", cfg->precision);
@@ -902,6 +911,7 @@ static int create_impl(const aw_config* cfg, aw_state_s* h) {
     if (h->kn.vn && cfg->ehrenfest)
       return fail(AW_E_ARG, "von Neumann batches record trace and purity only (no per-step Ehrenfest observables)");
   }
+  if (check_only) return AW_OK;
   h->active.assign(h->ni, 1);
   h->vmin_i.assign(h->ni, 0.0);
   h->kmin_i.assign(h->ni, 0.0);
@@ -1071,6 +1081,20 @@ extern "C" int aw_create(const aw_config* cfg, aw_handle* out) {
     return r;
   }
   *out = h;
+  return AW_OK;
+}
+
+extern "C" int aw_check_config(const aw_config* cfg, const char* arch) {
+  if (!cfg) return fail(AW_E_ARG, "null argument");
+  std::unique_ptr<aw_state_s> h(new aw_state_s());
+  TRY(create_impl(cfg, h.get(), true));
+  const std::string opt = std::string("--gpu-architecture=") + (arch && *arch ? arch : "sm_103a");
+  std::vector<char> cubin;
+  TRY(nvrtc_cubin(awjit::module_source(h->kn, h->consts, h->V, h->K, h->absx, h->absp, h->obs_x, h->obs_p,
+                                       h->pnames, h->init_expr),
+                  opt.c_str(), &cubin));
+  TRY(nvrtc_cubin(awjit::init_source(h->kn, h->consts, "1."), opt.c_str(), &cubin));
+  TRY(nvrtc_cubin(awjit::observable_source(h->kn, h->consts, "X"), opt.c_str(), &cubin));
   return AW_OK;
 }
 

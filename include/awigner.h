@@ -149,6 +149,11 @@ int aw_profile_read(aw_handle h, double* ms4, double* bytes4, int64_t* launches4
  * V_min and K_min (wigner_bloch_cuda_1d.py:70-92, rho_bloch_cuda_1d.py:70-98). */
 int aw_create(const aw_config* cfg, aw_handle* out);
 int aw_destroy(aw_handle h);
+/* The checks of aw_create without a device: the configuration is validated and the expression
+ * strings are compiled with NVRTC for `arch` ("sm_103a" when null or empty), which is where the
+ * reference's constructors raise a CompileError (SourceModule in wigner_moyal_cuda_1d.py:241-247).
+ * Nothing is allocated and no CUDA runtime call is made, so it runs on a machine without a GPU. */
+int aw_check_config(const aw_config* cfg, const char* arch);
 int aw_stream(aw_handle h, void** stream);
 int aw_sync(aw_handle h);
 int aw_bloch_min(aw_handle h, double* v_min, double* k_min);
