@@ -110,3 +110,26 @@ def test_errors_surface_as_the_constructor_raises_them():
     from accuratewigner_gb300 import _common
 
     assert getattr(_common._CHECK, "arch", None) is None
+
+
+def test_native_validation_without_a_device():
+    """The argument checks of aw_create, reached through the device-free check."""
+    from accuratewigner_gb300 import check_config
+    from _cases import VN, WM_ANHARMONIC
+
+    c = _classes()
+    small = dict(WM_ANHARMONIC, X_gridDIM=16)
+    with pytest.raises(AssertionError, match="grid sides"):
+        check_config(c["wm"], **small)
+    with pytest.raises(AssertionError, match="taken by the kernels"):
+        check_config(c["wm"], n_inst=4, batch_params=["X"], batch_init="1.", **WM_ANHARMONIC)
+    with pytest.raises(AssertionError, match="not an identifier"):
+        check_config(c["wm"], n_inst=4, batch_params=["2a"], batch_init="1.", **WM_ANHARMONIC)
+    with pytest.raises(AssertionError, match="do not depend on t"):
+        check_config(c["wm"], n_inst=4, batch_params=["a"], batch_init="1.",
+                     **dict(WM_ANHARMONIC, V="0.5 * X * X + a * X * sin(t)"))
+    with pytest.raises(AssertionError, match="trace and purity only"):
+        check_config(c["vn"], n_inst=4, batch_params=["a"], batch_init="1.", **VN)
+    # a batch whose per-instance constants appear in V, K and the initial state
+    check_config(c["wm"], n_inst=4, batch_params=["a"], batch_init="exp(-a * X * X - P * P)",
+                 **dict(WM_ANHARMONIC, V="0.5 * a * X * X"))
