@@ -50,6 +50,8 @@ def run_case(name, spec):
             out["K_min"] = obj.K_min
         elif verb == "ground":
             obj.set_ground_state(arg)
+        elif verb == "ground_state":
+            obj.get_ground_state(abs_tol_purity=arg)
         elif verb == "single_steps":
             for _ in range(arg):
                 obj.t += obj.dt

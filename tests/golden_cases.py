@@ -78,6 +78,35 @@ CASES = {
                          "exp(-sigma * pow(X_prime - x0, 2) - cuda_complex(0., p0) * X_prime)"],
              ["single_steps", 3], ["save", "rho_single"]],
     ),
+    # The cases below pin the oracle on the CPU only (gpu=False): the GPU library is checked against
+    # the oracle for the same features by test_rho_schrodinger_gpu.py (ordered von Neumann averages)
+    # and test_wigner_moyal_gpu.py / test_rho_schrodinger_gpu.py (ground states; their loops stop on
+    # purities that may differ from the reference's in the last digits, so those checks use 1e-8).
+    # von Neumann averages of ordered operator products (vn:520-563, kernel vn:811-821)
+    "vn_ordered_averages": dict(
+        kind="vn", gpu=False,
+        params=dict(t=0.0, dt=0.01, X_gridDIM=64, X_amplitude=8.0, sigma=1.0, p0=0.4, x0=0.5,
+                    K="0.5 * P * P", V="0.1 * X * X + 0.01 * X * X * X * X"),
+        ops=[["set_rho", "exp(-sigma * pow(X - x0, 2) + cuda_complex(0., p0) * X) * "
+                         "exp(-sigma * pow(X_prime - x0, 2) - cuda_complex(0., p0) * X_prime)"],
+             ["propagate", 6], ["average", ["x", ["X"]]], ["average", ["p", [None, "P"]]],
+             ["average", ["p2x", [None, "P * P", "X"]]], ["average", ["xpx", ["X", "P", "X"]]],
+             ["save", "purity"]],
+    ),
+    # Wigner-Bloch ground state with the dbeta-halving rollback (wb:157-219)
+    "wb_ground_state": dict(
+        kind="wb", gpu=False,
+        params=dict(t=0.0, dt=0.05, X_gridDIM=64, X_amplitude=6.0, P_gridDIM=64, P_amplitude=6.0, dbeta=0.05,
+                    K="0.5 * P * P", V="0.5 * X * X + 0.05 * X * X * X * X"),
+        ops=[["ground_state", 1e-8], ["save", "wigner"], ["save", "purity"]],
+    ),
+    # rho-Bloch ground state (rb:163-223)
+    "rb_ground_state": dict(
+        kind="rb", gpu=False,
+        params=dict(t=0.0, dt=0.05, X_gridDIM=64, X_amplitude=8.0, dbeta=0.05,
+                    K="0.5 * P * P", V="0.5 * X * X + 0.05 * X * X * X * X"),
+        ops=[["ground_state", 1e-8], ["save", "rho"], ["save", "purity"]],
+    ),
 }
 
 
@@ -109,6 +138,8 @@ def run_ops(obj, spec):
             out["K_min"] = obj.K_min
         elif verb == "ground":
             obj.set_ground_state(arg)
+        elif verb == "ground_state":
+            obj.get_ground_state(abs_tol_purity=arg)
         elif verb == "single_steps":
             for _ in range(arg):
                 obj.t += obj.dt

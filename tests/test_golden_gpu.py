@@ -15,7 +15,7 @@ def _gpu_cls(kind):
             "rb": aw.RhoBlochCUDA1D, "sw": aw.SchrodingerWignerCUDA1D}[kind]
 
 
-@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("name", sorted(n for n, spec in CASES.items() if spec.get("gpu", True)))
 def test_gpu_matches_reference_kernels(name):
     spec = CASES[name]
     obj = _gpu_cls(spec["kind"])(**spec["params"])
