@@ -133,3 +133,20 @@ def test_native_validation_without_a_device():
     # a batch whose per-instance constants appear in V, K and the initial state
     check_config(c["wm"], n_inst=4, batch_params=["a"], batch_init="exp(-a * X * X - P * P)",
                  **dict(WM_ANHARMONIC, V="0.5 * a * X * X"))
+
+
+def test_size_limits():
+    """Grid sides from 32 to 8192 (the von Neumann Wigner grid, 2N, up to 8192); wave functions up to 2^25."""
+    from accuratewigner_gb300 import check_config
+    from _cases import SW, VN, WM_ANHARMONIC
+
+    c = _classes()
+    check_config(c["wm"], **dict(WM_ANHARMONIC, X_gridDIM=8192, P_gridDIM=32))
+    with pytest.raises(AssertionError, match="grid sides"):
+        check_config(c["wm"], **dict(WM_ANHARMONIC, X_gridDIM=16384))
+    check_config(c["vn"], **dict(VN, X_gridDIM=4096))
+    with pytest.raises(AssertionError, match="grid sides"):
+        check_config(c["vn"], **dict(VN, X_gridDIM=8192))
+    check_config(c["sw"], **dict(SW, X_gridDIM=2 ** 25))
+    with pytest.raises(AssertionError):
+        check_config(c["sw"], **dict(SW, X_gridDIM=2 ** 26))
