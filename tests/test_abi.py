@@ -58,3 +58,23 @@ def test_classes_reject_bad_arguments_like_the_reference():
         WignerMoyalCUDA1D(X_gridDIM=100, P_gridDIM=64, X_amplitude=1.0, P_amplitude=1.0, V="X", K="P", dt=0.1)
     with pytest.raises(AttributeError, match="dt"):
         WignerMoyalCUDA1D(X_gridDIM=64, P_gridDIM=64, X_amplitude=1.0, P_amplitude=1.0, V="X", K="P")
+
+
+def test_header_compiles_as_c_and_the_library_serves_a_c_caller(lib, tmp_path):
+    """tests/c_abi_check.c: a C99 program against include/awigner.h, linked to libawigner.so."""
+    import shutil
+    import subprocess
+
+    from accuratewigner_gb300 import _lib
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    exe = str(tmp_path / "c_abi_check")
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "c_abi_check.c"), "-o", exe, "-L" + libdir, "-l:libawigner.so",
+                    "-Wl,-rpath," + libdir], check=True)
+    r = subprocess.run([exe], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout
+    assert "valid configuration: 0" in r.stdout
