@@ -33,6 +33,8 @@ AW_BUF_WIGNER = 1
 AW_BUF_PSI = 2
 AW_BUF_SNAPSHOT = 3
 
+AW_PROF_CLASSES = 5  # launch classes of aw_profile_read
+
 AW_TERM_X = 0
 AW_TERM_P = 1
 

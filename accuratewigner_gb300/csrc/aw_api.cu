@@ -218,11 +218,15 @@ struct aw_state_s {
     cudaEvent_t a, b;
   };
   bool prof_on = false;
+  bool prof_serial = false;  // side-stream launches go to the handle's stream while profiling
   std::vector<ProfRec> prof;
+  // the stream of the work that normally overlaps the next step (the handle's own while the profiler
+  // serialises launches, so that every event pair times one kernel alone)
+  cudaStream_t side() const { return prof_serial ? st : st2; }
 };
 
-// launch classes of the profiler
-enum { PROF_ROW = 0, PROF_COL = 1, PROF_JIT = 2, PROF_UTIL = 3, PROF_NCLS = 4 };
+// launch classes of the profiler (AW_PROF_CLASSES in awigner.h)
+enum { PROF_ROW = 0, PROF_COL = 1, PROF_JIT = 2, PROF_UTIL = 3, PROF_RED = 4, PROF_NCLS = 5 };
 
 static cudaEvent_t prof_mark(aw_state_s* h, cudaStream_t st = nullptr) {
   cudaEvent_t e = nullptr;
@@ -295,9 +299,12 @@ static int hjit(aw_state_s* h, cudaKernel_t k, dim3 g, dim3 b, void** args) { re
 
 extern "C" int aw_profile(aw_handle h, int32_t enable) {
   if (!h) return fail(AW_E_ARG, "null handle");
+  if (enable < 0 || enable > 2) return fail(AW_E_ARG, "aw_profile: mode must be 0, 1 or 2");
   cudaStreamSynchronize(h->st);
+  if (h->st2) cudaStreamSynchronize(h->st2);
   prof_clear(h);
   h->prof_on = enable != 0;
+  h->prof_serial = enable == 2;
   return AW_OK;
 }
 
@@ -600,7 +607,8 @@ static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row,
     r = row ? aw_launch_row_pass_f32(&a, batch, st) : aw_launch_col_pass_f32(&a, batch, st);
   else
     r = row ? aw_launch_row_pass_f64(&a, batch, st) : aw_launch_col_pass_f64(&a, batch, st);
-  prof_done(h, row ? PROF_ROW : PROF_COL, pass_bytes(h, a) * batch, pe, st);
+  const bool reduce_only = !row && !a.out && !a.mid_out && !a.br_out;
+  prof_done(h, row ? PROF_ROW : (reduce_only ? PROF_RED : PROF_COL), pass_bytes(h, a) * batch, pe, st);
   ++g_launches;
   if (r)
     return fail(AW_E_CUDA, "%s pass launch failed (%d, %s), grid %d x %d", row ? "row" : "column", r,
@@ -1785,6 +1793,7 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
   // normalize_rho_wigner (wm:608-622) is deferred to the end of the call: the step loop does not
   // wait for the reduction, which runs on a side stream.  Bloch steps normalise every step.
   const bool defer = !p.bloch && p.ehrenfest && h->st2;
+  cudaStream_t side = h->side();
   // With the deferred reduction the marginal pass of step n runs on the side stream as well, where
   // it overlaps the column and row passes of step n + 1 (and fills their last partial waves of
   // blocks).  The branch outputs then alternate between W and tmp, the last step's in W, so that a
@@ -1908,10 +1917,10 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       if (defer) {
         // after the row pass of step n, on the side stream: marginal pass, then the reduction
         CK(cudaEventRecord(h->ev_z[par], h->st));
-        CK(cudaStreamWaitEvent(h->st2, h->ev_z[par], 0));
-        TRY(col_pass(h, a, h->tw_c, h->st2));
-        TRY(launch_finalize_rot(h, times[n], hrow, 0, par, h->st2));
-        CK(cudaEventRecord(h->ev_f[par], h->st2));
+        CK(cudaStreamWaitEvent(side, h->ev_z[par], 0));
+        TRY(col_pass(h, a, h->tw_c, side));
+        TRY(launch_finalize_rot(h, times[n], hrow, 0, par, side));
+        CK(cudaEventRecord(h->ev_f[par], side));
       } else {
         TRY(col_pass(h, a, h->tw_c));
         TRY(launch_finalize_rot(h, times[n], hrow, p.stop_on_purity));

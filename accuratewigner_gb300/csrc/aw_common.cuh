@@ -10,7 +10,26 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "aw_df.cuh"
+
+// devices one process can drive (per-device records of the launchers)
+#define AW_MAX_DEVICES 64
+
+// Number of SMs of the current device, looked up once per device; grids are sized in multiples of
+// it (152 on GB300).
+inline int aw_sm_count() {
+  static std::atomic<int> cache[AW_MAX_DEVICES];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= AW_MAX_DEVICES) return 1;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) return 1;
+    cache[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
 
 template <typename T> struct cvec;
 template <> struct cvec<double> { typedef double2 type; };

@@ -18,7 +18,13 @@
 // The first call made on a device does the set-up: with that device current it
 // looks up the array's device address (cudaGetSymbolAddress) and keeps it for
 // later calls.  Make that first call on each device before any stream capture.
+// Later calls made outside stream capture look the address up again (cheap once
+// the module is loaded), so a cudaDeviceReset, after which the array lives at a
+// new address, is followed; a call made while its stream is being captured uses
+// the address kept by the last call outside capture.
 #include <cuda_runtime.h>
+
+#include <stdint.h>
 
 #include <mutex>
 #include <string>
@@ -121,14 +127,25 @@ extern "C" int aw_reduce_noalloc(const void* data, int32_t elem_bytes, int64_t n
     return nofail(AW_E_ARG, "aw_reduce_noalloc: at most 67108864 elements (1024 chunks of 65536, the size of its "
                             "static scratch); got " + std::to_string((long long)n));
   if (mode == 3 && stride <= 0) return nofail(AW_E_ARG, "aw_reduce_noalloc: the trace needs a positive stride");
+  // the trace reads element (n - 1) * stride: that index must exist as a 64-bit integer
+  if (mode == 3 && n > 1 && stride > (INT64_MAX / (n - 1)))
+    return nofail(AW_E_ARG, "aw_reduce_noalloc: (n - 1) * stride overflows a 64-bit index");
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return nofail(AW_E_CUDA, std::string("aw_reduce_noalloc: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= AW_NOALLOC_MAX_DEVICES) return nofail(AW_E_ARG, "aw_reduce_noalloc: device index too large");
+  cudaStream_t st = (cudaStream_t)stream;
+  // outside capture the address is looked up (again); inside, the kept one is used
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  const cudaError_t qe = cudaStreamIsCapturing(st, &cap);
+  if (qe != cudaSuccess) cudaGetLastError();  // a refused query (capture elsewhere) leaves no error behind
+  const bool capturing = qe != cudaSuccess || cap != cudaStreamCaptureStatusNone;
   double2* part;
   {
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_partials[dev]) {
+    if (!g_partials[dev] || !capturing) {
+      if (capturing)
+        return nofail(AW_E_ARG, "aw_reduce_noalloc: the first call on a device must come before stream capture");
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, aw_noalloc_partials);
       if (e != cudaSuccess)
@@ -137,7 +154,6 @@ extern "C" int aw_reduce_noalloc(const void* data, int32_t elem_bytes, int64_t n
     }
     part = g_partials[dev];
   }
-  cudaStream_t st = (cudaStream_t)stream;
   const int nchunks = (int)((n + AW_NOALLOC_CHUNK - 1) / AW_NOALLOC_CHUNK);
   if (nchunks > 0) k_chunk_partial<<<nchunks, 256, 0, st>>>(data, elem_bytes == 8, n, mode, stride, part);
   k_chunk_final<<<1, 256, 0, st>>>(part, nchunks, out_device);

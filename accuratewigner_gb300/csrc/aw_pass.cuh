@@ -8,6 +8,7 @@
 #pragma once
 #include <cooperative_groups.h>
 
+#include <atomic>
 #include <type_traits>
 
 #include "aw_common.cuh"
@@ -355,7 +356,7 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
 }
 
 // ------------------------------------------------------------------ dispatch
-static constexpr int AW_SMS = 152;
+// Grids are sized by the SM count of the device the launch goes to (aw_sm_count, aw_common.cuh).
 
 // rows per row-pass block: tiles of about 1024 elements
 inline int choose_row_lines(int ncols, int esz) {
@@ -369,7 +370,7 @@ inline int choose_row_lines(int ncols, int esz) {
 // of a wave function, whose nrows equals the tile)
 inline int choose_row_lines(int nrows, int ncols, int esz) {
   const int l = choose_row_lines(ncols, esz);
-  return (l > 1 && nrows > l && nrows / l < 2 * AW_SMS) ? 1 : l;
+  return (l > 1 && nrows > l && nrows / l < 2 * aw_sm_count()) ? 1 : l;
 }
 
 // columns per column-pass block: as many as fit (<= 16, <= 128 KB of shared memory, <= 512
@@ -384,19 +385,26 @@ inline int max_col_lines(int nrows, int ncols, int esz) {
 inline int choose_col_lines(int nrows, int ncols, int batch, int esz) {
   // as many columns as fit while the launch keeps at least 4 blocks per SM
   int b = max_col_lines(nrows, ncols, esz);
-  while (b > 1 && (long long)(ncols / b) * batch < 4 * AW_SMS) b >>= 1;
+  while (b > 1 && (long long)(ncols / b) * batch < 4 * aw_sm_count()) b >>= 1;
   return b;
 }
 
-// Opt a kernel in, once, to the dynamic shared memory its launches can ask for (tile plus, for a
-// clustered column pass, one row of FP64 partials), within the 227 KB per block of sm_103a.
+// Opt a kernel in to the dynamic shared memory its launches can ask for (tile plus, for a clustered
+// column pass, one row of FP64 partials), within the 227 KB per block of sm_103a.  The attribute
+// belongs to the device that is current, so it is set once per device: `slots` is the kernel's own
+// per-device record of the size granted (0: not yet set).
 template <typename K>
-static int prepare_smem(K kern, size_t max_dynamic) {
+static int prepare_smem(K kern, size_t max_dynamic, std::atomic<int>* slots) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= AW_MAX_DEVICES) return -3;
+  const int have = slots[dev].load(std::memory_order_acquire);
+  if (have > 0) return have;
   cudaFuncAttributes fa;
   if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess) return -3;
   const size_t cap = 227 * 1024 - fa.sharedSizeBytes;
   const size_t want = max_dynamic < cap ? max_dynamic : cap;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want) != cudaSuccess) return -3;
+  slots[dev].store((int)want, std::memory_order_release);
   return (int)want;
 }
 
@@ -410,8 +418,8 @@ static int launch_row_t(const AwPassArgs* a, int batch, cudaStream_t st) {
     if (a->nrows % LINES) return -2;
     const size_t smem = sizeof(V) * Tile::SMEM_ELEMS;
     auto kern = aw_pass_kernel<V, Tile, S::NT>;
-    static int max_dyn = prepare_smem(kern, smem);
-    if (max_dyn < (int)smem) return -3;
+    static std::atomic<int> granted[AW_MAX_DEVICES];
+    if (prepare_smem(kern, smem, granted) < (int)smem) return -3;
     dim3 grid(a->nrows / LINES, batch);
     kern<<<grid, S::NT, smem, st>>>(*a);
     return cudaGetLastError() == cudaSuccess ? 0 : -4;
@@ -432,11 +440,11 @@ static int launch_col_t(const AwPassArgs* a, int batch, cudaStream_t st) {
     const bool reduce_only = !a->out && !a->mid_out && !a->br_out && !a->f0.active && !a->d2 && !a->f2.active &&
                              !a->f3.active && !a->red_abs2 && (a->col_alt || a->alt_cross || a->red_line);
     auto kern = reduce_only ? aw_pass_kernel<V, Tile, S::NT, true> : aw_pass_kernel<V, Tile, S::NT, false>;
-    static int max_dyn = prepare_smem(aw_pass_kernel<V, Tile, S::NT, false>,
-                                      sizeof(V) * Tile::SMEM_ELEMS + sizeof(double2) * N);
-    static int max_dyn_r = prepare_smem(aw_pass_kernel<V, Tile, S::NT, true>,
-                                        sizeof(V) * Tile::SMEM_ELEMS + sizeof(double2) * N);
-    if ((reduce_only ? max_dyn_r : max_dyn) < (int)smem) return -3;
+    static std::atomic<int> granted[AW_MAX_DEVICES], granted_r[AW_MAX_DEVICES];
+    const size_t most = sizeof(V) * Tile::SMEM_ELEMS + sizeof(double2) * N;
+    const int max_dyn = reduce_only ? prepare_smem(aw_pass_kernel<V, Tile, S::NT, true>, most, granted_r)
+                                    : prepare_smem(aw_pass_kernel<V, Tile, S::NT, false>, most, granted);
+    if (max_dyn < (int)smem) return -3;
     dim3 grid(a->ncols / LINES, batch);
     if (!clustered) {
       kern<<<grid, S::NT, smem, st>>>(*a);

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "aw_common.cuh"
 #include "aw_util.h"
 
 namespace {
@@ -243,9 +244,11 @@ __global__ void k_set2(double* p, double a, double b) {
   p[1] = b;
 }
 
+// grid-stride launches: at most 32 blocks of 256 threads per SM of the current device
 inline int grid_for(long long n) {
   long long g = (n + 255) / 256;
-  if (g > 4 * 152 * 8) g = 4 * 152 * 8;
+  const long long cap = 32LL * aw_sm_count();
+  if (g > cap) g = cap;
   if (g < 1) g = 1;
   return (int)g;
 }

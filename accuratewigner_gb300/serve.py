@@ -15,9 +15,15 @@ Every request's computation is independent of the others in its pool, so a resul
 alone and in a mix up to the rounding of its chunk boundaries (a chunk ends with the state
 normalised, as propagate() does).
 
-Precision: an engine runs every request in complex128 ("c128"), in complex64 ("c64"), or picks per
-request ("auto"): complex64 when the error model below keeps the request's relative L2 error within
-its tolerance, complex128 (the FP64-accurate form) otherwise.
+Precision: an engine runs every request in complex128 ("c128" double-float or "c128-fp64" native
+FP64), in complex64 ("c64"), or picks per request ("auto") from a measurement: the request's first
+PROBE_STEPS steps run twice, in complex64 and in complex128, from the same initial state; the
+relative L2 distance of the two states is the measured complex64 error of the probe window, which is
+extrapolated to the request's full step count (FP32 rounding grows between a random walk, steps^0.5,
+and a drift, steps^1: the exponent C64_GROWTH bounds both).  A request whose estimate is within its
+tolerance continues in complex64 from the complex64 probe's state; otherwise it falls back and
+continues in complex128 from the complex128 probe's state, so that no step is run twice more than
+the probe window.  Every auto request records the estimate (est_error) and whether it fell back.
 """
 import collections
 import threading
@@ -43,16 +49,23 @@ INIT = {
 CLASSES = {"wm": WignerMoyalCUDA1D, "vn": RhoVNeumannCUDA1D, "rb": RhoBlochCUDA1D}
 
 
-# Relative L2 error of a complex64 propagation after `steps` steps on an n x n grid, against the FP64
-# result: the FP32 rounding of each FFT stage of the 4 propagation transforms a step adds up like a
-# random walk, err = C eps32 sqrt(4 steps log2 n).  C = 3 bounds the measured values (anharmonic
-# Wigner-Moyal 256^2, 1000 steps: 1.4e-5, C = 1.3; strong-field 1024^2, 1000 steps: 3.2e-5, C = 2.7).
-C64_ERROR_C = 3.0
+# Measured complex64 error of the probe window, extrapolated to the whole request:
+#   est = err(probe) * (steps / probe) ** C64_GROWTH
+# FP32 rounding of the butterflies adds up between a random walk (exponent 0.5) and a drift (1.0);
+# measured on the anharmonic 256^2 Wigner-Moyal run against FP64: 2.9e-6 after 100 steps, 7.0e-6
+# after 300, 1.5e-5 after 1000 (exponent 0.71), so 0.8 errs on the side of falling back.
+PROBE_STEPS = 200
+C64_GROWTH = 0.8
 EPS32 = 2.0 ** -24
+# a tolerance below this is out of complex64's reach whatever the step count (a few FP32 roundings)
+C64_MIN_TOL = 8.0 * EPS32
 
 
-def c64_error(n, steps):
-    return C64_ERROR_C * EPS32 * np.sqrt(4.0 * steps * np.log2(n))
+def c64_estimate(probe_err, probe_steps, steps):
+    """Estimated relative L2 error after `steps` steps from the error measured after `probe_steps`."""
+    if steps <= probe_steps:
+        return float(probe_err)
+    return float(probe_err) * (steps / float(probe_steps)) ** C64_GROWTH
 
 
 def amplitude(n):
@@ -82,6 +95,10 @@ class Request:
         self.history = []      # per-step observable rows (wm)
         self.purity = None
         self.state = None      # host copy of the final W (wm) or rho (vn, rb) when keep_state
+        self.init_rho = None   # start from this rho (host array) instead of the initial-state expression
+        self.est_error = None  # auto engines: estimated complex64 error of the whole request (measured)
+        self.fell_back = False  # auto engines: the estimate exceeded tol and the request finished in complex128
+        self.on_done = None    # internal requests of an auto engine: callback instead of the finished list
 
     @property
     def latency(self):
@@ -151,7 +168,10 @@ class Pool(threading.Thread):
                 req = self.queue.popleft()
             c2, c3, c4 = req.coeffs
             self.batch.set_params(s, [c2, c3, c4, req.x0, req.p0])
-            self.batch.init_state(s, 1)
+            if req.init_rho is None:
+                self.batch.init_state(s, 1)
+            else:
+                self.batch.set_rho(s, req.init_rho)
             req.start = time.perf_counter()
             self.occupant[s] = req
             self.left[s] = req.steps
@@ -182,11 +202,16 @@ class Pool(threading.Thread):
             req = self.occupant[s]
             if req.keep_state:
                 req.state = self.batch.wigner(s) if self.kind == "wm" else self.batch.rho(s)
+                if req.on_done is not None:
+                    req.rho = self.batch.rho(s)  # the continuation starts from rho
             if self.kind != "rb":
                 req.purity = self.batch.purity(s)
             req.done = time.perf_counter()
             self.occupant[s] = None
-            self.engine._finished(req)
+            if req.on_done is not None:
+                req.on_done(req)
+            else:
+                self.engine._finished(req)
 
     def run(self):
         try:
@@ -232,9 +257,10 @@ class Engine:
         return free
 
     def precision_for(self, req):
+        """The form a request starts in (auto: complex64 unless its tolerance is out of its reach)."""
         if self.precision != "auto":
             return self.precision
-        return "c64" if c64_error(req.n, req.steps) <= req.tol else "c128"
+        return "c64" if req.tol >= C64_MIN_TOL else "c128"
 
     def pool(self, kind, n, precision=None):
         """The pool of (kind, n, precision), created when the free device memory covers it."""
@@ -272,7 +298,65 @@ class Engine:
     # requests ---------------------------------------------------------------
     def submit(self, req):
         req.precision = self.precision_for(req)
+        if self.precision == "auto" and req.precision == "c64":
+            self._probe(req)
+            return
         self.pool(req.kind, req.n, req.precision).submit(req)
+
+    # auto: the measured complex64 error and the fallback -------------------------
+    def _sub(self, req, steps, precision, init_rho, on_done):
+        r = Request(req.rid, req.kind, req.n, steps, req.coeffs, req.x0, req.p0, arrival=req.arrival,
+                    keep_state=True, tol=req.tol)
+        r.precision = precision
+        r.init_rho = init_rho
+        r.on_done = on_done
+        self.pool(r.kind, r.n, precision).submit(r)
+        return r
+
+    def _probe(self, req):
+        """Run the first PROBE_STEPS steps of `req` in complex64 and in complex128; when both are done,
+        continue in the form the measured error allows (see the module docstring)."""
+        probe = min(PROBE_STEPS, req.steps)
+        lock = threading.Lock()
+        got = {}
+
+        def probe_done(r):
+            with lock:
+                got[r.precision] = r
+                if len(got) < 2:
+                    return
+            lo, hi = got["c64"], got["c128"]
+            ref = hi.state
+            err = float(np.linalg.norm(lo.state - ref) / max(np.linalg.norm(ref), 1e-300))
+            # a Gibbs run that stopped early (purity 1) ends with its probe
+            stopped = hi.steps_done < probe or lo.steps_done < probe
+            req.est_error = c64_estimate(err, probe, probe if stopped else req.steps)
+            keep = lo if req.est_error <= req.tol else hi
+            req.fell_back = keep is hi
+            req.precision = keep.precision
+            req.history = list(keep.history)
+            req.steps_done = keep.steps_done
+            req.start = min(lo.start, hi.start)
+            left = req.steps - probe
+            if stopped or left <= 0:
+                self._complete(req, keep, continued=False)
+                return
+            self._sub(req, left, keep.precision, keep.rho, lambda c: self._complete(req, c, continued=True))
+
+        self._sub(req, probe, "c64", None, probe_done)
+        self._sub(req, probe, "c128", None, probe_done)
+
+    def _complete(self, req, last, continued):
+        """Finish an auto request from its last internal request: the probe it kept, or the
+        continuation after it (whose steps and observable rows follow the probe's)."""
+        if continued:
+            req.history.extend(last.history)
+            req.steps_done += last.steps_done
+        req.purity = last.purity
+        if req.keep_state:
+            req.state = last.state
+        req.done = time.perf_counter()
+        self._finished(req)
 
     def _finished(self, req):
         with self.done_cv:

@@ -81,8 +81,9 @@ INIT = "exp(-X * X - P * P) / M_PI"
 CHUNK = 50  # steps per propagate() call, as the reference's own driver loop (wigner_moyal_cuda_1d.py:954)
 
 STATE_BYTES_PER_PT = {"c128": 16, "c128-fp64": 16, "c64": 8}
+METRIC = "grid-pt*steps/s (Wigner-Moyal split step with per-step Wigner transform and Ehrenfest observables)"
 # arithmetic of the passes per precision
-DTYPE = {"c128": "c128 state, f32x2 double-float arithmetic", "c128-fp64": "f64", "c64": "f32+f64",
+DTYPE = {"c128": "f32x2 (double-float pairs; complex128 state)", "c128-fp64": "f64", "c64": "f32 (FP64 tables and sums)",
          "auto": "per request: c64 (f32+f64) within the error bound, else c128"}
 ALG_BYTES_FACTOR = 10  # bytes per grid point per step = 10 * S (propagation 4 S + per-step Wigner transform 6 S)
 
@@ -143,22 +144,144 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_propagator(precision):
-    from accuratewigner_gb300 import WignerBlochCUDA1D, WignerMoyalCUDA1D
+def make_propagator(precision, init=None):
+    """The headline propagator on the headline initial state (or on `init`, a Wigner function)."""
+    from accuratewigner_gb300 import WignerMoyalCUDA1D
 
-    # Gibbs state of the field-free soft-core atom (kT = 1) as the initial condition
-    gibbs_params = {k: v for k, v in PARAMS.items() if k not in ("diff_K", "diff_V", "abs_boundary_x")}
-    gibbs_params.update(kT=1.0, dbeta=0.05, precision="c128")
-    wb = WignerBlochCUDA1D(**gibbs_params)
-    w0 = wb.get_gibbs_state().get()
-    wb.close()
     prop = WignerMoyalCUDA1D(**PARAMS, precision=precision)
-    prop.set_wignerfunction(w0)
+    prop.set_wignerfunction(INIT if init is None else init)
     return prop
 
 
 def flush_l2(buf):
     buf.add_(1.0)
+
+
+def headline_config(world):
+    """The `config` of the headline line: the same dictionary for both arms."""
+    return {
+        "workload": "strong-field Wigner-Moyal, 1024x1024 (x,p), X_amplitude=60, P_amplitude=6, soft-core V + "
+                    "x E(t), dt=0.05, cos^(1/8) absorber, Ehrenfest every step",
+        "grid": [N_GRID, N_GRID],
+        "precision": "complex128 state, FP64 arithmetic",
+        "steps_per_call": CHUNK,
+        "initial_state": "exp(-x^2 - p^2)/pi (synthetic, in place of the beta=100 Wigner-Bloch ground state)",
+        "l2": "flushed (256 MB write) before every timed propagate() call; the 48 MB working set (state and two "
+              "branch buffers) stays L2-resident within a call",
+        "parallelism": "replicas" if world > 1 else "single GPU",
+        "algorithmic_bytes_per_pt_step": ALG_BYTES_FACTOR * 16,
+    }
+
+
+DATA = ("synthetic: the 1024x1024 strong-field configuration with the Gaussian exp(-x^2-p^2)/pi as initial "
+        "state in place of the beta=100 Wigner-Bloch ground state (timing does not depend on the state)")
+# per launch of each pass kind, bytes read + written per grid point in units of S (the element size):
+# the row pass reads and writes the state and writes the branch output; the column pass reads and
+# writes the state; the marginal pass reads the branch output only
+PASS_UNITS = {"row_pass": 3, "column_pass": 2, "marginal_pass": 1}
+CLASS_OF = {"row_pass": 0, "column_pass": 1, "marginal_pass": 4}
+
+
+def kernel_profile(lib, h, precision, peak):
+    """One extra propagate() of CHUNK steps with CUDA events around every launch, the overlapped side
+    stream folded into the handle's stream so that every event pair times one kernel alone; per pass
+    kind: launches, mean duration, algorithmic bytes per launch and the achieved fraction of `peak`."""
+    from accuratewigner_gb300 import _lib
+
+    ncls = _lib.AW_PROF_CLASSES
+    _lib.check(lib.aw_profile(h, 2))
+    t = ctypes.c_double(0.0)
+    _lib.check(lib.aw_propagate(h, CHUNK, ctypes.byref(t)))
+    ms = (ctypes.c_double * ncls)()
+    by = (ctypes.c_double * ncls)()
+    nl = (ctypes.c_int64 * ncls)()
+    _lib.check(lib.aw_profile_read(h, ms, by, nl))
+    _lib.check(lib.aw_profile(h, 0))
+    S = STATE_BYTES_PER_PT[precision]
+    out = {}
+    for name, cls in CLASS_OF.items():
+        n = int(nl[cls])
+        if not n:
+            continue
+        mean_ms = ms[cls] / n
+        alg = PASS_UNITS[name] * S * N_GRID * N_GRID
+        gbs = alg / (mean_ms / 1e3) / 1e9
+        out[name] = {"launches": n, "mean_us": mean_ms * 1e3, "total_ms": ms[cls], "alg_bytes_per_launch": alg,
+                     "achieved_gbs": gbs, "frac": gbs / peak}
+    other = {"expression": 2, "helper": 3}
+    out["other"] = {k: {"launches": int(nl[c]), "total_ms": ms[c]} for k, c in other.items()}
+    return out
+
+
+def roofline_of(prof, precision, peak, peaks):
+    """The roofline object of the dominant kernel (largest total time among the passes)."""
+    passes = {k: v for k, v in prof.items() if k in PASS_UNITS}
+    dom = max(passes, key=lambda k: passes[k]["total_ms"])
+    d = passes[dom]
+    return {
+        "bound": "hbm",
+        "kernel": dom,
+        "achieved": d["achieved_gbs"],
+        "peak": peak,
+        "unit": "GB/s",
+        "frac": d["frac"],
+        "traffic": load_traffic(dom, precision),
+        "alg_bytes_per_launch": d["alg_bytes_per_launch"],
+        "mean_launch_us": d["mean_us"],
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s",
+        "per_kernel": {k: {"mean_us": v["mean_us"], "achieved_gbs": v["achieved_gbs"], "frac": v["frac"],
+                           "alg_bytes_per_launch": v["alg_bytes_per_launch"], "launches": v["launches"],
+                           "traffic": load_traffic(k, precision)} for k, v in passes.items()},
+        "timing": "CUDA events around every launch of one extra %d-step propagate() after the timed region, "
+                  "the overlapping side stream folded into the handle's stream (each event pair times one "
+                  "kernel alone)" % CHUNK,
+        "note": "the 48 MB working set stays in L2 within a call; the passes are bound by the FP64 pipe "
+                "(native FP64) or by FP32 issue and latency (double-float), not by HBM: see fp64_pipe",
+    }
+
+
+def time_chunks(lib, h, prop, chunks, l2buf, stream):
+    """CUDA-event time of each propagate() call on the library's stream, L2 flushed before each."""
+    import torch
+
+    times = []
+    for n in chunks:
+        flush_l2(l2buf)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        t = ctypes.c_double(prop.t)
+        from accuratewigner_gb300 import _lib
+
+        _lib.check(lib.aw_propagate(h, int(n), ctypes.byref(t)))
+        prop.t = np.float64(t.value)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    return times
+
+
+def accuracy_vs_fp64(steps=1000):
+    """W relative L2 after `steps` steps and the largest error of <x>, <p> and the dipole acceleration
+    over the steps (relative to max(|FP64|, 1)) of the double-float and complex64 forms against the
+    native FP64 form, all three from the headline initial state."""
+    runs = {}
+    for prec in ("c128-fp64", "c128", "c64"):
+        g = make_propagator(prec)
+        for _ in range(steps // CHUNK):
+            g.propagate(CHUNK)
+        runs[prec] = (g.wignerfunction.get(), {k: np.array(getattr(g, k)) for k in ("X_average", "P_average",
+                                                                                    "P_average_RHS")})
+        g.close()
+    w_ref, o_ref = runs["c128-fp64"]
+    out = {}
+    for prec in ("c128", "c64"):
+        w, o = runs[prec]
+        err = {k: float(np.max(np.abs(o[k] - o_ref[k]) / np.maximum(np.abs(o_ref[k]), 1.0))) for k in o}
+        out[prec] = {"steps": steps, "W_rel_l2": float(np.linalg.norm(w - w_ref) / np.linalg.norm(w_ref)),
+                     "x": err["X_average"], "p": err["P_average"], "dipole_acceleration": err["P_average_RHS"]}
+    return out
 
 
 def run_ours(args):
@@ -174,75 +297,55 @@ def run_ours(args):
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     lib = _lib.load()
-    prop = make_propagator(args.precision)
-    h = prop._h
-    st = ctypes.c_void_p()
-    _lib.check(lib.aw_stream(h, ctypes.byref(st)))
-    stream = torch.cuda.ExternalStream(st.value)
-    l2buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
-    npts = N_GRID * N_GRID
-
-    def propagate_raw(n):
-        t = ctypes.c_double(prop.t)
-        _lib.check(lib.aw_propagate(h, int(n), ctypes.byref(t)))
-        prop.t = np.float64(t.value)
-
-    # warm-up
-    propagate_raw(max(args.warmup, 3))
-    torch.cuda.synchronize()
-
-    chunks = []
-    left = args.steps
-    while left > 0:
-        chunks.append(min(CHUNK, left))
-        left -= chunks[-1]
-    launches0 = _lib.launch_count()
-    times = []
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        for n in chunks:
-            flush_l2(l2buf)
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            propagate_raw(n)
-            e1.record(stream)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1) / 1e3)
-    torch.cuda.synchronize()
-    launches = _lib.launch_count() - launches0
-    from accuratewigner_gb300.replicas import job_throughput
-
-    # replicas: the slowest rank's time, the work of all ranks
-    total, _, value = job_throughput(float(sum(times)), npts * args.steps, device="cuda")
-    if dist:
-        dist.barrier()
-
-    # per-kernel timing of one chunk (separate run, events around every launch)
-    _lib.check(lib.aw_profile(h, 1))
-    propagate_raw(CHUNK)
-    ms = (ctypes.c_double * 4)()
-    by = (ctypes.c_double * 4)()
-    nl = (ctypes.c_int64 * 4)()
-    _lib.check(lib.aw_profile_read(h, ms, by, nl))
-    _lib.check(lib.aw_profile(h, 0))
-    classes = ["row_pass", "column_pass", "expression", "helper"]
-    prof = {c: {"ms": ms[i], "bytes": by[i], "launches": int(nl[i])} for i, c in enumerate(classes)}
-    dom = max(range(2), key=lambda i: ms[i])
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = by[dom] / (ms[dom] / 1e3) / 1e9 if ms[dom] > 0 else None
-    traffic = load_traffic(classes[dom], args.precision)
+    l2buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+    npts = N_GRID * N_GRID
+    chunks = []
+    left = args.steps
+    while left > 0:
+        chunks.append(min(CHUNK, left))
+        left -= chunks[-1]
 
-    # end-to-end through the public API with host buffers: per chunk upload rho from
-    # pinned host memory, propagate, read back the Wigner function and the observables
+    def measure(precision, clocked):
+        prop = make_propagator(precision)
+        h = prop._h
+        st = ctypes.c_void_p()
+        _lib.check(lib.aw_stream(h, ctypes.byref(st)))
+        stream = torch.cuda.ExternalStream(st.value)
+        t = ctypes.c_double(prop.t)
+        _lib.check(lib.aw_propagate(h, max(args.warmup, 3), ctypes.byref(t)))  # warm-up
+        prop.t = np.float64(t.value)
+        torch.cuda.synchronize()
+        launches0 = _lib.launch_count()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        if clocked:
+            with ClockSampler(local) as clk:
+                times = time_chunks(lib, h, prop, chunks, l2buf, stream)
+            clocks = clk.summary()
+        else:
+            times, clocks = time_chunks(lib, h, prop, chunks, l2buf, stream), None
+        torch.cuda.synchronize()
+        launches = _lib.launch_count() - launches0
+        from accuratewigner_gb300.replicas import job_throughput
+
+        total, _, value = job_throughput(float(sum(times)), npts * args.steps, device="cuda")
+        if dist:
+            dist.barrier()
+        prof = kernel_profile(lib, h, precision, peak)
+        return prop, {"value": value, "ms_per_step": total / args.steps * 1e3, "launches": int(launches),
+                      "clocks": clocks, "profile": prof, "roofline": roofline_of(prof, precision, peak, peaks)}
+
+    prop, main = measure(args.precision, True)
+
+    # end-to-end through the public API with host buffers: per chunk upload rho from pinned host memory,
+    # propagate, read back the Wigner function and the observables
     host_rho = torch.empty((N_GRID, N_GRID), dtype=torch.complex128, pin_memory=True).numpy()
     host_rho[:] = prop.rho.get()
     e2e_times = []
@@ -256,55 +359,56 @@ def run_ours(args):
         _ = prop.X_average[-n:], prop.P_average[-n:], prop.P_average_RHS[-n:]
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
+    prop.close()
+    from accuratewigner_gb300.replicas import job_throughput
+
     e2e_total, _, e2e_value = job_throughput(float(sum(e2e_times)), npts * args.steps, device="cuda")
-    S = STATE_BYTES_PER_PT[args.precision]
     h2d = npts * 16 * len(chunks) / args.steps
     d2h = (npts * 16 + CHUNK * 7 * 8) * len(chunks) / args.steps
+
+    # the other two arithmetic forms of the same step, each with its own time and roofline, and their
+    # errors against native FP64
+    forms = {}
+    if not args.no_forms:
+        for prec in ("c128-fp64", "c128", "c64"):
+            if prec == args.precision:
+                continue
+            p2, m = measure(prec, False)
+            p2.close()
+            forms[prec] = {"dtype": DTYPE[prec], "value": m["value"], "ms_per_step": m["ms_per_step"],
+                           "roofline": {k: m["roofline"][k] for k in ("kernel", "achieved", "frac", "per_kernel")}}
+        if world == 1:
+            acc = accuracy_vs_fp64()
+            for prec, e in acc.items():
+                if prec in forms:
+                    forms[prec]["error_vs_fp64"] = e
 
     if rank == 0:
         cpu = cpu_baseline(args) if world == 1 and not args.no_cpu else None
         line = {
-            "metric": "grid-pt*steps/s (Wigner-Moyal split step with per-step Wigner transform and Ehrenfest observables)",
-            "value": value,
+            "metric": METRIC,
+            "value": main["value"],
             "unit": "grid-pt*steps/s",
             "n_gpus": world,
             "steps": args.steps,
             "warmup": args.warmup,
-            "ms_per_step": total / args.steps * 1e3,
+            "ms_per_step": main["ms_per_step"],
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
             "dtype": DTYPE[args.precision],
-            "data": "synthetic (the 1024x1024 strong-field shapes; Gibbs-state initial condition)",
-            "config": {
-                "workload": "strong-field Wigner-Moyal, 1024x1024 (x,p), X_amplitude=60, P_amplitude=6, soft-core V + "
-                            "x E(t), dt=0.05, cos^(1/8) absorber, Ehrenfest every step",
-                "precision": args.precision,
-                "grid": [N_GRID, N_GRID],
-                "steps_per_call": CHUNK,
-                "l2": "flushed (256 MB write) before every timed propagate() call; the 48 MB working set "
-                      "(state and two branch buffers) stays L2-resident within a call",
-                "parallelism": "replicas" if world > 1 else "single GPU",
-                "algorithmic_bytes_per_pt_step": ALG_BYTES_FACTOR * S,
-            },
+            "data": DATA,
+            "config": headline_config(world),
             "e2e": {"value": e2e_value, "unit": "grid-pt*steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "gpu_launches": int(launches),
-            "roofline": {
-                "bound": "hbm",
-                "kernel": classes[dom],
-                "achieved": achieved,
-                "peak": peak,
-                "unit": "GB/s",
-                "frac": (achieved / peak) if achieved else None,
-                "traffic": traffic,
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s",
-                "note": "the passes are bound by the latency and FP32 issue of their double-float arithmetic "
-                        "(native FP64: by the FP64 pipe), not by HBM; the 48 MB working set stays in L2 within a "
-                        "call; frac is the HBM fraction of the dominant pass",
-            },
-            "kernel_profile": prof,
-            "clocks": clk.summary(),
+            "gpu_launches": main["launches"],
+            "roofline": main["roofline"],
+            "fp64_pipe": fp64_pipe_note(args.precision),
+            "kernel_profile": main["profile"],
+            "forms": forms,
+            "clocks": main["clocks"],
         }
+        if args.precision != "c128-fp64":
+            line["config"]["precision"] = DTYPE[args.precision]
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))
@@ -312,11 +416,22 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def load_traffic(kernel_class, precision):
-    """DRAM bytes per launch of the dominant pass, from the committed ncu summary (or None)."""
+def fp64_pipe_note(precision):
+    """FP64-pipe figures of the passes from the committed ncu capture, for the native FP64 form."""
+    if precision != "c128-fp64":
+        return None
     path = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
     try:
-        return json.load(open(path)).get("%s/%s" % (kernel_class, precision))
+        return json.load(open(path)).get("fp64_pipe")
+    except Exception:
+        return None
+
+
+def load_traffic(kernel, precision):
+    """DRAM bytes per launch of a pass kind, from the committed ncu summary (or None)."""
+    path = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
+    try:
+        return json.load(open(path)).get("%s/%s" % (kernel, precision))
     except Exception:
         return None
 
@@ -325,8 +440,7 @@ def cpu_baseline(args, steps=2):
     """The oracle (NumPy + pocketfft, all host cores) on a bounded sample of the workload."""
     from oracle import propagators as orc
 
-    p = dict(PARAMS)
-    params = {k: v for k, v in p.items() if k != "functions"}
+    params = {k: v for k, v in PARAMS.items() if k != "functions"}
     o = orc.WignerMoyalOracle(**params, py_functions={"E": e_field, "cosmask": cosmask})
     o.set_wignerfunction(INIT)
     o.propagate(1)
@@ -357,7 +471,7 @@ def run_reference(args):
     value = N_GRID * N_GRID * sample * args.steps / total
     line = {
         "impl": "reference",
-        "metric": "grid-pt*steps/s (Wigner-Moyal split step with per-step Wigner transform and Ehrenfest observables)",
+        "metric": METRIC,
         "value": value,
         "unit": "grid-pt*steps/s",
         "n_gpus": world,
@@ -368,10 +482,8 @@ def run_reference(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic (the 1024x1024 strong-field shapes)",
-        "config": {"workload": "strong-field Wigner-Moyal, 1024x1024 (x,p), X_amplitude=60, P_amplitude=6, soft-core V "
-                               "+ x E(t), dt=0.05, cos^(1/8) absorber, Ehrenfest every step",
-                   "precision": "c128", "grid": [N_GRID, N_GRID]},
+        "data": DATA,
+        "config": headline_config(world),
         "cpu_baseline": {"value": value, "unit": "grid-pt*steps/s", "cores": orc.WORKERS, "kind": "port",
                          "sample": "one split step per timed step (NumPy restatement of the reference, scipy.fft "
                                    "workers=%d)" % orc.WORKERS},
@@ -614,11 +726,15 @@ def run_large_vn(args):
     from accuratewigner_gb300 import RhoVNeumannCUDA1D
 
     n, steps = 4096, args.steps if args.steps != 200 else 2000
-    p = dict(t=0.0, dt=0.02, X_gridDIM=n, X_amplitude=80.0, D=0.18, alpha=1.0, xm=1.4, K="0.5 * P * P",
-             V="D * pow(1. - exp(-alpha * (X - xm)), 2) + X * 0.02 * sin(0.01 * t)", diff_K="P",
-             diff_V="2. * D * alpha * exp(-alpha * (X - xm)) * (1. - exp(-alpha * (X - xm))) + 0.02 * sin(0.01 * t)")
+    # the Morse wall capped at 1e4 (it reaches 9e69 at x = -80, where kick phases would depend on the
+    # last bits of V); states in the well move as under the uncapped wall
+    morse = "D * pow(1. - exp(-alpha * (X - xm)), 2)"
+    p = dict(t=0.0, dt=0.02, X_gridDIM=n, X_amplitude=80.0, D=0.18, alpha=1.0, xm=1.4, Vcap=1e4, K="0.5 * P * P",
+             V="fmin(%s, Vcap) + X * 0.02 * sin(0.01 * t)" % morse, diff_K="P",
+             diff_V="2. * D * alpha * exp(-alpha * (X - xm)) * (1. - exp(-alpha * (X - xm))) * (%s < Vcap)"
+                    " + 0.02 * sin(0.01 * t)" % morse)
     rng = np.random.default_rng(0)
-    centres = rng.uniform(-3.0, 6.0, 8)
+    centres = rng.uniform(0.5, 4.0, 8)
     w = rng.uniform(0.2, 1.0, 8)
     w /= w.sum()
     x = np.linspace(-80.0, 80.0 - 160.0 / n, n)
@@ -650,7 +766,8 @@ def run_large_vn(args):
         extra["vs_c128"] = {"rho_rel_l2": float(np.linalg.norm(rho - rref) / np.linalg.norm(rref)),
                             "x_max_abs_err": float(np.max(np.abs(xav - xref))), "purity_err": float(abs(pur - pref))}
     _line("large-vn", "grid-pt*steps/s", n * n * steps / sec, "grid-pt*steps/s", sec, args,
-          {"grid": [n, n], "X_amplitude": 80.0, "dt": 0.02, "steps": steps, "initial": "8 Gaussians, seed 0",
+          {"grid": [n, n], "X_amplitude": 80.0, "dt": 0.02, "steps": steps, "potential": "Morse capped at 1e4",
+           "initial": "8 Gaussians, centres U(0.5, 4), seed 0",
            "precision": args.precision}, extra)
 
 
@@ -660,8 +777,9 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="c128", choices=["c128", "c128-fp64", "c64", "auto"])
+    ap.add_argument("--precision", default="c128-fp64", choices=["c128", "c128-fp64", "c64", "auto"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="headline: skip the other arithmetic forms")
     ap.add_argument("--workload", default="strong-field",
                     choices=["strong-field", "plain", "batched-gibbs", "served", "served-sweep", "large-vn",
                              "precision", "frames"])

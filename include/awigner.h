@@ -134,11 +134,17 @@ int64_t aw_launch_count(void);
 
 /* Timing of the handle's own launches with CUDA events (no counterpart in the
  * reference, which has no timers).  aw_profile(h, 1) clears and starts
- * recording; aw_profile_read fills, per launch class (0 row passes, 1 column
- * passes, 2 expression kernels, 3 helper kernels), the summed device time in
- * ms, the summed algorithmic HBM bytes and the launch count. */
+ * recording with every launch on its usual stream; aw_profile(h, 2) does the
+ * same but puts the work that normally overlaps the next step (the marginal
+ * pass and observable reduction of Wigner-Moyal steps) on the handle's own
+ * stream, so that each event pair times one kernel running alone;
+ * aw_profile(h, 0) stops.  aw_profile_read fills, per launch class (0 row
+ * passes, 1 column passes that store, 2 expression kernels, 3 helper kernels,
+ * 4 reduction-only column passes), the summed device time in ms, the summed
+ * algorithmic HBM bytes and the launch count: arrays of AW_PROF_CLASSES. */
+#define AW_PROF_CLASSES 5
 int aw_profile(aw_handle h, int32_t enable);
-int aw_profile_read(aw_handle h, double* ms4, double* bytes4, int64_t* launches4);
+int aw_profile_read(aw_handle h, double* ms, double* bytes, int64_t* launches);
 
 /* Construction: replaces the __init__ of each propagator class
  * (wigner_moyal_cuda_1d.py:17-327, wigner_bloch_cuda_1d.py:19-68,
@@ -242,10 +248,14 @@ int aw_sw_ehrenfest(aw_handle h, double t, double* row);
  * aw_purity (mode 1: Sum Re(a*a)), |a|^2 (mode 2) and aw_trace (mode 3: Sum of
  * a[k * stride], k < n), over n complex128 (elem_bytes 16) or complex64 (8)
  * elements at `data`; writes out_device[0..1] = (re, im), stream-ordered on
- * `stream`.  Scratch is a 16 KiB static device array: at most 67108864
- * elements per call (larger n is rejected with AW_E_ARG).  The first call on a
- * device looks up that array's address; make it before any stream capture.
- * Calls overlapping on the GPU race on the shared array. */
+ * `stream`.  For the trace the buffer must hold (n - 1) * stride + 1 elements
+ * (an index that overflows 64 bits is rejected with AW_E_ARG).  Scratch is a
+ * 16 KiB static device array: at most 67108864 elements per call (larger n is
+ * rejected with AW_E_ARG).  The first call on a device looks up that array's
+ * address; make it before any stream capture.  Later calls outside capture
+ * look it up again (it moves after cudaDeviceReset); calls inside capture use
+ * the address kept by the last call outside it.  Calls overlapping on the GPU
+ * race on the shared array. */
 int aw_reduce_noalloc(const void* data, int32_t elem_bytes, int64_t n, int64_t stride, int32_t mode,
                       double* out_device, void* stream);
 

@@ -24,8 +24,9 @@ import subprocess
 
 import numpy as np
 
-REF = os.environ.get("AW_REFERENCE_DIR", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
+# the reference checkout: $AW_REFERENCE_DIR, else a folder named "reference" beside this repository
+REF = os.environ.get("AW_REFERENCE_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 OUT = os.path.join(HERE, "_ref")
 SHIM = os.path.join(HERE, "ref_shim")
 

@@ -78,3 +78,20 @@ def test_header_compiles_as_c_and_the_library_serves_a_c_caller(lib, tmp_path):
     r = subprocess.run([exe], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     assert r.returncode == 0, r.stdout
     assert "valid configuration: 0" in r.stdout
+
+
+def test_noalloc_argument_checks_need_no_device(lib):
+    """aw_reduce_noalloc rejects bad arguments before any CUDA call: an oversized input, an unknown
+    mode and a trace whose last index (n - 1) * stride overflows 64 bits."""
+    import ctypes
+
+    from accuratewigner_gb300 import _lib
+
+    p = ctypes.c_void_p(16)  # never dereferenced: every call below fails its argument checks
+    assert lib.aw_reduce_noalloc(p, 16, 67108864 + 1, 0, 0, p, None) == _lib.AW_E_ARG
+    assert b"67108864" in lib.aw_last_error()
+    assert lib.aw_reduce_noalloc(p, 16, 8, 0, 4, p, None) == _lib.AW_E_ARG
+    assert lib.aw_reduce_noalloc(p, 12, 8, 0, 0, p, None) == _lib.AW_E_ARG
+    assert lib.aw_reduce_noalloc(p, 16, 3, 2 ** 62, 3, p, None) == _lib.AW_E_ARG
+    assert b"overflows" in lib.aw_last_error()
+    assert lib.aw_reduce_noalloc(p, 16, 3, 0, 3, p, None) == _lib.AW_E_ARG

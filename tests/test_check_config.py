@@ -150,3 +150,16 @@ def test_size_limits():
     check_config(c["sw"], **dict(SW, X_gridDIM=2 ** 25))
     with pytest.raises(AssertionError):
         check_config(c["sw"], **dict(SW, X_gridDIM=2 ** 26))
+
+
+def test_benchmark_configuration_parity_cases():
+    """The benchmark-size parity configurations (plain 256^2, strong field 1024^2, capped-Morse von
+    Neumann 4096^2) compile for sm_103a."""
+    from accuratewigner_gb300 import check_config
+    from test_baseline_configs_gpu import FIELD_C, PLAIN, STRONG, VN4096
+
+    c = _classes()
+    check_config(c["wm"], **PLAIN)
+    check_config(c["wm"], precision="c64", **PLAIN)
+    check_config(c["wm"], functions=FIELD_C, **STRONG)
+    check_config(c["vn"], **VN4096)

@@ -22,3 +22,20 @@ def test_gpu_matches_reference_kernels(name):
     got = run_ops(obj, spec)
     bad = compare(got, load_golden(name), TOL)
     assert not bad, bad
+
+
+# The golden cases held on the CPU oracle only: the ordered von Neumann averages at the plain bar, and the
+# Wigner-Bloch / rho-Bloch ground states at 1e-8 (their loops end on purity thresholds, wb:178 and rb:184,
+# that rounding in the last digits can move by a step; the reference's dbeta-halving rollback is part of
+# what is compared).
+GROUND_TOL = 1e-8
+
+
+@pytest.mark.parametrize("name", sorted(n for n, spec in CASES.items() if not spec.get("gpu", True)))
+def test_gpu_matches_reference_kernels_cpu_only_cases(name):
+    spec = CASES[name]
+    obj = _gpu_cls(spec["kind"])(**spec["params"])
+    got = run_ops(obj, spec)
+    tol = GROUND_TOL if any(op[0] == "ground_state" for op in spec["ops"]) else TOL
+    bad = compare(got, load_golden(name), tol)
+    assert not bad, bad

@@ -65,12 +65,15 @@ def test_served_wigner_moyal_matches_the_plain_propagator():
     assert obs_close(h[:, 0], s.X_average, 1e-10)
 
 
-def test_auto_precision_meets_each_request_tolerance():
-    from accuratewigner_gb300.serve import Engine, Request
+def test_auto_precision_measures_the_complex64_error_and_falls_back():
+    """An auto engine runs each request's probe window in complex64 and complex128, keeps complex64
+    when the extrapolated measured error is within the request's tolerance, and otherwise falls back
+    to complex128 from the complex128 probe's state (then the result is the complex128 one)."""
+    from accuratewigner_gb300.serve import C64_MIN_TOL, Engine, Request
 
     def reqs():
-        return [Request(0, "wm", 64, 30, (0.5, 0.01, 0.02), 0.5, -0.3, keep_state=True, tol=1e-5),
-                Request(1, "vn", 64, 400, (0.3, 0.0, 0.01), -0.7, 0.4, keep_state=True, tol=1e-9)]
+        return [Request(0, "wm", 64, 400, (0.5, 0.01, 0.02), 0.5, -0.3, keep_state=True, tol=1e-3),
+                Request(1, "vn", 64, 1000, (0.3, 0.0, 0.01), -0.7, 0.4, keep_state=True, tol=C64_MIN_TOL)]
 
     auto = reqs()
     eng = Engine(precision="auto", chunk=50, slots={64: 2})
@@ -80,6 +83,13 @@ def test_auto_precision_meets_each_request_tolerance():
     e2 = Engine(precision="c128", chunk=50, slots={64: 2})
     e2.run(ref, realtime=False)
     e2.close()
-    assert auto[0].precision == "c64" and auto[1].precision == "c128"
+    loose, tight = auto
+    assert loose.precision == "c64" and not loose.fell_back and loose.est_error <= loose.tol
+    assert tight.precision == "c128" and tight.fell_back and tight.est_error > tight.tol
     for a, r in zip(auto, ref):
+        assert a.steps_done == r.steps_done == a.steps
         assert rel_l2(a.state, r.state) <= a.tol, (a.rid, rel_l2(a.state, r.state))
+    # the fallback continued the complex128 trajectory: the same as complex128 throughout
+    assert rel_l2(tight.state, ref[1].state) < 1e-10
+    hm, hr = np.concatenate(loose.history), np.concatenate(ref[0].history)
+    assert hm.shape == hr.shape == (400, hm.shape[1])

@@ -30,15 +30,79 @@ def test_pool_memory_grows_with_side_and_slots():
         assert abs((2 * a / n) ** 2 - 2 * np.pi / n) < 1e-12
 
 
-def test_auto_precision_routes_by_the_error_model():
-    from accuratewigner_gb300.serve import Engine, Request, c64_error
+class _FakePool:
+    """Runs a request at once on the host: complex128 gives the state `base`, complex64 the same state
+    with a relative error `c64_err`; records every request it was given."""
+
+    def __init__(self, engine, precision, base, c64_err, log):
+        self.engine, self.precision, self.base, self.c64_err, self.log = engine, precision, base, c64_err, log
+
+    def submit(self, r):
+        import numpy as np
+
+        self.log.append(r)
+        state = self.base * (1.0 + (self.c64_err if self.precision == "c64" else 0.0))
+        r.start = 0.0
+        r.steps_done = r.steps
+        r.history = [np.full((r.steps, 3), 1.0 if self.precision == "c64" else 2.0)]
+        r.state = state
+        r.rho = state
+        r.purity = 0.5
+        r.done = 1.0
+        (r.on_done or self.engine._finished)(r)
+
+
+def _auto_engine(c64_err):
+    import numpy as np
+
+    from accuratewigner_gb300.serve import Engine
 
     eng = Engine(precision="auto")
-    short = Request(0, "wm", 128, 50, (0.5, 0.0, 0.0), tol=1e-5)
-    long = Request(1, "wm", 2048, 5000, (0.5, 0.0, 0.0), tol=1e-5)
-    loose = Request(2, "vn", 2048, 5000, (0.5, 0.0, 0.0), tol=1e-3)
-    assert c64_error(128, 50) <= 1e-5 < c64_error(2048, 5000) <= 1e-3
-    assert eng.precision_for(short) == "c64"
-    assert eng.precision_for(long) == "c128"
-    assert eng.precision_for(loose) == "c64"
-    assert Engine(precision="c128").precision_for(short) == "c128"
+    log = []
+    base = np.ones((4, 4), np.complex128)
+    eng.pool = lambda kind, n, precision=None: _FakePool(eng, precision, base, c64_err, log)
+    return eng, log
+
+
+def test_auto_falls_back_to_complex128_on_the_measured_error():
+    """A request whose extrapolated complex64 error exceeds its tolerance continues in complex128
+    from the complex128 probe's state; the estimate is recorded."""
+    from accuratewigner_gb300.serve import C64_GROWTH, PROBE_STEPS, Request
+
+    eng, log = _auto_engine(c64_err=1e-6)
+    tight = Request(0, "wm", 128, 1000, (0.5, 0.0, 0.0), tol=2e-6)
+    eng.submit(tight)
+    assert [r.precision for r in log] == ["c64", "c128", "c128"]
+    assert [r.steps for r in log] == [PROBE_STEPS, PROBE_STEPS, 1000 - PROBE_STEPS]
+    assert log[2].init_rho is log[1].rho  # continued from the complex128 probe
+    assert tight.fell_back and tight.precision == "c128"
+    assert abs(tight.est_error - 1e-6 * (1000 / PROBE_STEPS) ** C64_GROWTH) < 1e-12
+    assert tight.steps_done == 1000 and tight.done is not None
+    assert eng.finished == [tight]
+
+
+def test_auto_keeps_complex64_within_tolerance():
+    from accuratewigner_gb300.serve import PROBE_STEPS, Request
+
+    eng, log = _auto_engine(c64_err=1e-6)
+    loose = Request(1, "vn", 256, 1000, (0.5, 0.0, 0.0), tol=1e-3)
+    eng.submit(loose)
+    assert [r.precision for r in log] == ["c64", "c128", "c64"]
+    assert log[2].init_rho is log[0].rho  # continued from the complex64 probe
+    assert not loose.fell_back and loose.precision == "c64" and loose.est_error < 1e-3
+    # the probe's observable rows come first, then the continuation's
+    assert len(loose.history) == 2 and loose.history[0].shape[0] == PROBE_STEPS
+    # a request no longer than the probe window ends with it
+    eng2, log2 = _auto_engine(c64_err=1e-6)
+    short = Request(2, "wm", 128, 50, (0.5, 0.0, 0.0), tol=1e-5)
+    eng2.submit(short)
+    assert [r.steps for r in log2] == [50, 50] and short.precision == "c64" and short.steps_done == 50
+
+
+def test_auto_routes_unreachable_tolerances_to_complex128():
+    from accuratewigner_gb300.serve import C64_MIN_TOL, Engine, Request
+
+    eng = Engine(precision="auto")
+    assert eng.precision_for(Request(0, "wm", 128, 50, (0.5, 0.0, 0.0), tol=C64_MIN_TOL / 2)) == "c128"
+    assert eng.precision_for(Request(0, "wm", 128, 50, (0.5, 0.0, 0.0), tol=1e-5)) == "c64"
+    assert Engine(precision="c128").precision_for(Request(0, "wm", 128, 50, (0.5, 0.0, 0.0))) == "c128"

@@ -60,6 +60,42 @@ def test_noalloc_matches_sum_purity_trace_twice():
         assert abs(tr - ref_tr) <= TOL * max(1.0, abs(ref_tr))
 
 
+@pytest.mark.parametrize("elem_bytes", [16, 8])
+def test_noalloc_several_chunks_all_modes_against_numpy(elem_bytes):
+    """Inputs of several 65536-element chunks plus a remainder, so that the per-chunk partials are
+    written and then summed in order; every mode, complex128 and complex64, each call twice (a stale
+    partial of the first call, or of the larger call before it, would show in the second)."""
+    import torch
+
+    from accuratewigner_gb300 import _lib
+
+    lib = _lib.load()
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    rng = np.random.default_rng(11)
+    ctype = np.complex128 if elem_bytes == 16 else np.complex64
+    tdtype = torch.complex128 if elem_bytes == 16 else torch.complex64
+    n_big = 5 * 65536 + 3
+    n = 3 * 65536 + 17
+    stride = 3
+    host = (rng.standard_normal((n - 1) * stride + 1) + 1j * rng.standard_normal((n - 1) * stride + 1)).astype(ctype)
+    dev = torch.from_numpy(host).to("cuda")
+    big = torch.from_numpy((rng.standard_normal(n_big) + 1j * rng.standard_normal(n_big)).astype(ctype)).to("cuda")
+    assert dev.dtype == tdtype
+    a = host[:n].astype(np.complex128)
+    diag = host[::stride][:n].astype(np.complex128)
+    want = {0: (a.sum(), np.abs(a).sum()),
+            1: (complex((a.real ** 2 - a.imag ** 2).sum()), (np.abs(a) ** 2).sum()),
+            2: (complex((np.abs(a) ** 2).sum()), (np.abs(a) ** 2).sum()),
+            3: (diag.sum(), np.abs(diag).sum())}
+    for mode in range(4):
+        # a larger call first leaves partials in chunks the next call does not use
+        _reduce(lib, big.data_ptr(), elem_bytes, n_big, 1, mode, out)
+        for _ in range(2):
+            got = _reduce(lib, dev.data_ptr(), elem_bytes, n, stride if mode == 3 else 0, mode, out)
+            ref, scale = want[mode]
+            assert abs(got - ref) <= 1e-12 * scale, (mode, got, ref)
+
+
 def test_noalloc_rejects_oversized_input():
     from accuratewigner_gb300 import _lib
 
