@@ -17,10 +17,23 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libawigner.so")
 
-# the double-float pass kernels are the slowest to compile: one unit per line length, started first
-DF_SIZES = [32, 64, 128, 256, 512, 1024, 2048, 4096, 8192]
-SOURCES = (["aw_pass_df_%d.cu" % n for n in DF_SIZES] +
-           ["aw_api.cu", "aw_util.cu", "aw_pass_f64.cu", "aw_pass_f32.cu", "aw_pass_df.cu", "aw_noalloc.cu"])
+# The pass kernels of each arithmetic form and line length compile in a unit of their own, generated
+# into _build/gen/ (an include of aw_pass.cuh and one AW_SIZE_LAUNCHERS line), largest first.
+SIZES = [8192, 4096, 2048, 1024, 512, 256, 128, 64, 32]
+FORMS = [("df", "dfc"), ("f64", "double2"), ("f32", "float2")]
+SOURCES = ["aw_api.cu", "aw_util.cu", "aw_pass_dispatch.cu", "aw_noalloc.cu"]
+GEN = os.path.join(BUILD, "gen")
+
+
+def _generated():
+    """(path, text) of every generated pass unit."""
+    out = []
+    for n in SIZES:
+        for tag, vt in FORMS:
+            text = "// generated by _build.py: %s pass kernels of line length %d\n" % (tag, n)
+            text += '#include "aw_pass.cuh"\n\nAW_SIZE_LAUNCHERS(%s, %s, %d)\n' % (vt, tag, n)
+            out.append((os.path.join(GEN, "aw_pass_%s_%d.cu" % (tag, n)), text))
+    return out
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
@@ -54,19 +67,26 @@ def _run(cmd):
 
 
 def build(force=False, verbose=False):
-    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(GEN, exist_ok=True)
     deps = _deps()
     jobs = []
     objs = []
-    for src in SOURCES:
-        s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+    units = []
+    for path, text in _generated():
+        if not os.path.exists(path) or open(path).read() != text:
+            with open(path, "w") as f:
+                f.write(text)
+        units.append(path)
+    units += [os.path.join(CSRC, src) for src in SOURCES]
+    for s in units:
+        o = os.path.join(BUILD, os.path.basename(s).replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + deps):
             jobs.append([_nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                                             "-I" + INCLUDE, "-I" + CSRC, "-c", s, "-o", o])
     if jobs:
-        with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        workers = min(len(jobs), max(2, (os.cpu_count() or 4)))
+        with ThreadPoolExecutor(max_workers=workers) as ex:
             for out in ex.map(_run, jobs):
                 if verbose and out.strip():
                     sys.stderr.write(out)

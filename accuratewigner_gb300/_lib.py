@@ -94,6 +94,8 @@ SIGNATURES = [
     ("aw_last_error", c_cp, []),
     ("aw_launch_count", c_i64, []),
     ("aw_profile", c_int, [c_vp, c_int]),
+    ("aw_graph", c_int, [c_vp, c_int]),
+    ("aw_pass_form", c_int, [c_vp, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
     ("aw_profile_read", c_int, [c_vp, ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl), ctypes.POINTER(c_i64)]),
     ("aw_create", c_int, [ctypes.POINTER(AwConfig), ctypes.POINTER(c_vp)]),
     ("aw_destroy", c_int, [c_vp]),

@@ -138,6 +138,13 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
+// steps of one captured window of the Wigner-Moyal step loop: as many of a call's steps as fit (even,
+// since the branch outputs alternate), from AW_GRAPH_MIN to AW_GRAPH_MAX (its tables and times fit
+// the 256 slots of the time-dependent kick tables); AW_GRAPH_CACHE windows are kept per handle
+#define AW_GRAPH_MIN 16
+#define AW_GRAPH_MAX 248
+#define AW_GRAPH_CACHE 4
+
 struct aw_state_s {
   aw_config cfg;
   std::string consts, V, K, absx, absp;
@@ -160,6 +167,21 @@ struct aw_state_s {
   int col_lines = 0;                   // columns per column-pass block of a batch (fixed, so that an
                                        // instance computes the same way whatever the view)
   int tuned_col_lines = 0;             // ... of the propagation column pass, chosen by timing (tune_col_lines)
+  int tuned_col_tma = 0;               // ... and whether its tile is staged by TMA (chosen the same way)
+  int tuned_col_shape = 0;             // ... and its elements a thread (AwPassArgs.shape)
+  int tuned_row_shape = 0;             // elements a thread of the propagation row pass (tune_row_shape)
+  int* err_host = nullptr;             // error word of the pass kernels' bounded waits (mapped pinned memory)
+  // the Wigner-Moyal step loop replayed from CUDA graphs of windows of steps (rot_run), captured on
+  // first use per (window length, parity of the call's step count), least recently used dropped
+  bool graph_on = true;
+  cudaGraphExec_t graph_exec[AW_GRAPH_CACHE] = {};
+  long long graph_key[AW_GRAPH_CACHE] = {};
+  long long graph_used[AW_GRAPH_CACHE] = {};
+  long long graph_launches[AW_GRAPH_CACHE] = {};
+  long long graph_clock = 0;
+  DevBuf hwin;                         // history rows of one window
+  DevBuf ctimes;                       // step times of the current call
+  int* err_dev = nullptr;              // ... its device address
   cudaKernel_t k_binit = nullptr;
   // buffers currently holding double-float state (pointer, elements); plain complex128 at rest
   std::vector<std::pair<void*, long long>> df_live;
@@ -224,6 +246,8 @@ struct aw_state_s {
   // serialises launches, so that every event pair times one kernel alone)
   cudaStream_t side() const { return prof_serial ? st : st2; }
 };
+
+
 
 // launch classes of the profiler (AW_PROF_CLASSES in awigner.h)
 enum { PROF_ROW = 0, PROF_COL = 1, PROF_JIT = 2, PROF_UTIL = 3, PROF_RED = 4, PROF_NCLS = 5 };
@@ -598,6 +622,7 @@ static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row,
     if (!row && !a.lines_hint) a.lines_hint = h->col_lines;
   }
   if (row && !a.row_lines) a.row_lines = row_lines(h, a.nrows, a.ncols);
+  a.err = h->err_dev;
   if (h->df) TRY(df_prepare(h, a, batch, st));
   cudaEvent_t pe = prof_mark(h, st);
   int r;
@@ -610,6 +635,8 @@ static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row,
   const bool reduce_only = !row && !a.out && !a.mid_out && !a.br_out;
   prof_done(h, row ? PROF_ROW : (reduce_only ? PROF_RED : PROF_COL), pass_bytes(h, a) * batch, pe, st);
   ++g_launches;
+  if (r == -9) return fail(AW_E_STATE, "%s pass: no kernel of the other shape for %d x %d", row ? "row" : "column",
+                          a.nrows, a.ncols);
   if (r)
     return fail(AW_E_CUDA, "%s pass launch failed (%d, %s), grid %d x %d", row ? "row" : "column", r,
                 cudaGetErrorString(cudaGetLastError()), a.nrows, a.ncols);
@@ -709,24 +736,33 @@ static std::string cstr(const char* s, const char* dflt) { return s ? std::strin
 static std::mutex g_tune_mu;
 static std::map<std::tuple<int, int, int, int>, int> g_tuned;
 
+static AwFactor fshear_x(aw_state_s* h);
 static AwFactor fshear_y(aw_state_s* h);
 
 static int tune_col_lines(aw_state_s* h) {
   if (h->kn.sw) return AW_OK;
-  const auto key = std::make_tuple(h->nr, h->nc, h->ni, h->df ? 2 : (h->f32 ? 1 : 0));
+  const auto key = std::make_tuple(h->nr, h->nc, h->ni, (h->df ? 2 : (h->f32 ? 1 : 0)) + 4 * h->tuned_col_shape);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tuned.find(key);
     if (it != g_tuned.end()) {
-      h->tuned_col_lines = it->second;
+      h->tuned_col_lines = it->second & 0xff;
+      h->tuned_col_tma = (it->second >> 8) & 1;
       return AW_OK;
     }
   }
   const int bmax = aw_col_pass_max_lines(h->nr, h->nc, h->f32);
+  // candidates: (columns per block) + 256 * (tile staged by TMA), in the column shape chosen for the
+  // grid and form (tune_shapes, + 512 when it is the other one); TMA boxes need rows of 16-byte
+  // multiples; a width without a kernel of that shape is dropped when it is tried
   std::vector<int> cand;
-  for (int b = 1; b <= bmax; b *= 2) cand.push_back(b);
+  const int sh = 512 * h->tuned_col_shape;
+  for (int b = 1; b <= bmax; b *= 2) {
+    cand.push_back(b + sh);
+    if ((b * h->esz) % 16 == 0) cand.push_back(b + 256 + sh);
+  }
   int best = cand.empty() ? 1 : cand[0];
-  if (cand.size() > 1) {
+  if (cand.size() > 1 || h->tuned_col_shape) {
     CK(cudaMemsetAsync(h->tmp.p, 0, (size_t)h->ni * gsz(h) * h->esz, h->st));
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -741,8 +777,15 @@ static int tune_col_lines(aw_state_s* h) {
         a.d1 = -1;
         a.f1 = fshear_y(h);  // a table read and two complex multiplies per point, as a phase kick
         a.d2 = +1;
-        a.lines_hint = cand[c];
+        a.lines_hint = cand[c] & 0xff;
+        a.tma = (cand[c] >> 8) & 1;
+        a.shape = cand[c] >> 9;
+        if (best_of[c] < 0.f) continue;  // no kernel of this shape
         int r = col_pass(h, a, h->tw_c);  // warm-up (first launch of this instantiation)
+        if (r == AW_E_STATE) {
+          best_of[c] = -1.f;
+          continue;
+        }
         float ms = 0.f;
         if (!r) {
           cudaEventRecord(e0, h->st);
@@ -759,9 +802,10 @@ static int tune_col_lines(aw_state_s* h) {
         if (round == 0 || ms < best_of[c]) best_of[c] = ms;
       }
     }
-    size_t bi = 0;
-    for (size_t c = 1; c < cand.size(); ++c)
-      if (best_of[c] < best_of[bi]) bi = c;
+    size_t bi = cand.size();
+    for (size_t c = 0; c < cand.size(); ++c)
+      if (best_of[c] >= 0.f && (bi == cand.size() || best_of[c] < best_of[bi])) bi = c;
+    if (bi == cand.size()) return fail(AW_E_STATE, "no column-pass kernel for a %d x %d grid", h->nr, h->nc);
     best = cand[bi];
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -769,12 +813,129 @@ static int tune_col_lines(aw_state_s* h) {
   }
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tuned[key] = best;
-  h->tuned_col_lines = best;
+  h->tuned_col_lines = best & 0xff;
+  h->tuned_col_tma = (best >> 8) & 1;
+  return AW_OK;
+}
+
+// Elements a thread (and so the FFT radix) of the propagation row and column passes, timed once per
+// (grid, form) in this process: each pass as ifft, a table kick and fft, in both shapes (where the
+// other exists).  A shape changes the FFT's rounding (radix-4 and radix-8 stages round differently),
+// so the choice is one per grid and form for the whole process, the same for a single propagator and
+// for a batch of any size; columns per block and TMA staging are then tuned per handle.
+static std::map<std::tuple<int, int, int>, std::pair<int, int>> g_tuned_shapes;
+
+static int tune_shapes(aw_state_s* h) {
+  if (h->kn.sw) return AW_OK;
+  const auto key = std::make_tuple(h->nr, h->nc, h->df ? 2 : (h->f32 ? 1 : 0));
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned_shapes.find(key);
+    if (it != g_tuned_shapes.end()) {
+      h->tuned_row_shape = it->second.first;
+      h->tuned_col_shape = it->second.second;
+      return AW_OK;
+    }
+  }
+  float best_of[2][2] = {{0.f, 0.f}, {0.f, 0.f}};  // [row, column][shape], < 0: no kernel
+  CK(cudaMemsetAsync(h->tmp.p, 0, (size_t)gsz(h) * h->esz, h->st));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  int r = AW_OK;
+  for (int round = 0; round < 3 && r == AW_OK; ++round)
+    for (int pass = 0; pass < 2 && r == AW_OK; ++pass)
+      for (int shape = 0; shape < 2 && r == AW_OK; ++shape) {
+        if (best_of[pass][shape] < 0.f) continue;
+        const bool row = pass == 0;
+        AwPassArgs a = pnone(h);
+        a.in = a.out = h->tmp.p;
+        a.d1 = -1;
+        a.f1 = row ? fshear_x(h) : fshear_y(h);  // a table read and two complex multiplies per point
+        a.d2 = +1;
+        a.shape = shape;
+        if (row) a.row_lines = row_lines(h, h->nr, h->nc);
+        r = launch_pass(h, a, row ? h->tw_r : h->tw_c, row);
+        if (r == AW_E_STATE) {  // no kernel of this shape for the grid
+          best_of[pass][shape] = -1.f;
+          r = AW_OK;
+          continue;
+        }
+        float ms = 0.f;
+        if (!r) {
+          cudaEventRecord(e0, h->st);
+          for (int k = 0; k < 4 && !r; ++k) r = launch_pass(h, a, row ? h->tw_r : h->tw_c, row);
+          cudaEventRecord(e1, h->st);
+          cudaEventSynchronize(e1);
+          cudaEventElapsedTime(&ms, e0, e1);
+        }
+        if (round == 0 || ms < best_of[pass][shape]) best_of[pass][shape] = ms;
+      }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (r) return r;
+  TRY(settle(h));
+  const int row_best = (best_of[0][1] >= 0.f && best_of[0][1] < best_of[0][0]) ? 1 : 0;
+  const int col_best = (best_of[1][1] >= 0.f && best_of[1][1] < best_of[1][0]) ? 1 : 0;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tuned_shapes.find(key);  // another handle may have tuned first: its choice stands
+  if (it == g_tuned_shapes.end()) it = g_tuned_shapes.emplace(key, std::make_pair(row_best, col_best)).first;
+  h->tuned_row_shape = it->second.first;
+  h->tuned_col_shape = it->second.second;
   return AW_OK;
 }
 
 // Bloch minima of instance i: min over (V(x) + V(x')) = min V(x) + min V(x') since rounding is
 // monotone (the reference's V_min / K_min, wigner_bloch_cuda_1d.py:55-92)
+// forget the captured step-loop graphs (recaptured on next use)
+static void drop_graphs(aw_state_s* h) {
+  for (auto& g : h->graph_exec)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+// The propagation passes' forms (no counterpart in the reference), as chosen by the autotuner:
+// form[0] columns per column-pass block, form[1] TMA staging of the column tile, form[2] elements a
+// thread of the column pass (0 by the size rule, 1 the other), form[3] the same for the row pass.  Entries
+// of `set` below zero keep the current choice; `get` receives the forms in force.
+extern "C" int aw_pass_form(aw_handle h, const int32_t* set, int32_t* get) {
+  if (!h) return fail(AW_E_ARG, "null handle");
+  if (set) {
+    const int lines = set[0] > 0 ? set[0] : h->tuned_col_lines;
+    const int tma = set[1] >= 0 ? set[1] : h->tuned_col_tma;
+    const int bmax = aw_col_pass_max_lines(h->nr, h->nc, h->f32);
+    if ((lines & (lines - 1)) || lines > bmax || h->nc % lines)
+      return fail(AW_E_ARG, "aw_pass_form: columns per block must be a power of two dividing %d, at most %d", h->nc,
+                  bmax);
+    if (tma && (lines * h->esz) % 16)
+      return fail(AW_E_ARG, "aw_pass_form: TMA boxes need rows of a multiple of 16 bytes (%d columns of %d bytes)",
+                  lines, h->esz);
+    if (set[2] > 1 || set[3] > 1) return fail(AW_E_ARG, "aw_pass_form: shapes are 0 or 1");
+    h->tuned_col_lines = lines;
+    h->tuned_col_tma = tma != 0;
+    if (set[2] >= 0) h->tuned_col_shape = set[2];
+    if (set[3] >= 0) h->tuned_row_shape = set[3];
+    drop_graphs(h);  // captured launches carry the old forms
+  }
+  if (get) {
+    get[0] = h->tuned_col_lines;
+    get[1] = h->tuned_col_tma;
+    get[2] = h->tuned_col_shape;
+    get[3] = h->tuned_row_shape;
+  }
+  return AW_OK;
+}
+
+extern "C" int aw_graph(aw_handle h, int32_t enable) {
+  if (!h) return fail(AW_E_ARG, "null handle");
+  CK(cudaStreamSynchronize(h->st));
+  drop_graphs(h);
+  h->graph_on = enable != 0;
+  return AW_OK;
+}
+
 static int bloch_minima(aw_state_s* h, int i) {
   const aw_config* cfg = &h->cfg;
   const int nmax = std::max(h->nr, h->nc);
@@ -926,6 +1087,13 @@ static int create_impl(const aw_config* cfg, aw_state_s* h, bool check_only = fa
   h->minima_ok.assign(h->ni, 0);
 
   CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+  // graph windows by default where launch latency is a large part of a step (measured on GB300 with
+  // Ehrenfest observables: 256^2 complex64 -26 %, native FP64 -19 %, double-float +-1 %; at 1024^2
+  // within 1 % for complex128 and 5 % slower for complex64)
+  h->graph_on = (long long)h->nr * h->nc <= 512LL * 512;
+  CK(cudaHostAlloc((void**)&h->err_host, sizeof(int), cudaHostAllocMapped));
+  *h->err_host = 0;
+  CK(cudaHostGetDevicePointer((void**)&h->err_dev, h->err_host, 0));
   if (h->kn.rotated) {
     CK(cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking));
     for (int k = 0; k < 2; ++k) {
@@ -1066,6 +1234,7 @@ static int create_impl(const aw_config* cfg, aw_state_s* h, bool check_only = fa
     if (cfg->absp_mode) TRY(dalloc(h->maskp, ni * grid * (h->f32 ? 4 : 8)));
   }
 
+  TRY(tune_shapes(h));
   TRY(tune_col_lines(h));
 
   if (h->kind == AW_WIGNER_BLOCH || h->kind == AW_RHO_BLOCH) {
@@ -1113,10 +1282,14 @@ extern "C" int aw_destroy(aw_handle h) {
                     &h->vseq, &h->vtimes, &h->zbuf, &h->altbuf, &h->twist_hi, &h->twist_lo, &h->rho, &h->W, &h->snap, &h->tmp, &h->stage, &h->tw_r, &h->tw_c, &h->tw_w, &h->shx_hi,
                     &h->shx_lo, &h->shy_hi, &h->shy_lo, &h->tabs, &h->maskx, &h->maskp, &h->red_line,
                     &h->red_cross, &h->red_sq, &h->rowsum, &h->diag, &h->abs2, &h->scal, &h->stop, &h->hist,
-                    &h->terms, &h->part, &h->blk_tabs, &h->params, &h->bvec, &h->maskx2, &h->masksep};
+                    &h->terms, &h->part, &h->blk_tabs, &h->params, &h->bvec, &h->maskx2, &h->masksep,
+                    &h->hwin, &h->ctimes};
   for (DevBuf* b : bufs) dfree(*b);
   for (DevBuf& b : h->sw_states) dfree(b);
+  for (auto& g : h->graph_exec)
+    if (g) cudaGraphExecDestroy(g);
   if (h->st) cudaStreamDestroy(h->st);
+  if (h->err_host) cudaFreeHost(h->err_host);
   if (h->st2) {
     cudaStreamSynchronize(h->st2);
     cudaStreamDestroy(h->st2);
@@ -1136,10 +1309,21 @@ extern "C" int aw_stream(aw_handle h, void** stream) {
   return AW_OK;
 }
 
+// A pass kernel whose bounded wait ran out (its TMA copies did not arrive) records a code in the
+// handle's error word and skips its tile; the next call that synchronises reports it.
+static int check_err(aw_state_s* h) {
+  if (!h->err_host) return AW_OK;
+  const int code = *(volatile int*)h->err_host;
+  if (!code) return AW_OK;
+  *(volatile int*)h->err_host = 0;
+  return fail(AW_E_CUDA, "a pass kernel's bounded wait for its TMA tile copies ran out (code %d); the results of "
+                         "the call that launched it are incomplete", code);
+}
+
 extern "C" int aw_sync(aw_handle h) {
   if (!h) return fail(AW_E_ARG, "null handle");
   CK(cudaStreamSynchronize(h->st));
-  return AW_OK;
+  return check_err(h);
 }
 
 extern "C" int aw_bloch_min(aw_handle h, double* v_min, double* k_min) {
@@ -1247,7 +1431,7 @@ extern "C" int aw_get_buffer(aw_handle h, int32_t which, void* dst, int32_t dst_
     }
   }
   CK(cudaStreamSynchronize(h->st));
-  return AW_OK;
+  return check_err(h);
 }
 
 extern "C" int aw_copy_buffer(aw_handle h, int32_t from, int32_t to) {
@@ -1528,7 +1712,7 @@ static double* abs2_of(aw_state_s* h, int par) { return (double*)h->abs2.p + (si
 static double* hist_of(aw_state_s* h, int i) { return (double*)h->hist.p + (size_t)i * h->hist_cap * h->hist_cols; }
 
 static int launch_finalize_rot(aw_state_s* h, double t, double* hist_row, int stop_on_purity, int par = 0,
-                               cudaStream_t st = nullptr) {
+                               cudaStream_t st = nullptr, const double* tptr = nullptr) {
   // every instance of the view: blockIdx.y = instance - v0
   const int i0 = h->v0;
   int nparts = h->z_blocks;
@@ -1556,7 +1740,8 @@ static int launch_finalize_rot(aw_state_s* h, double t, double* hist_row, int st
   int nchunk = std::max(1, std::min(64, std::min(ncol, nrow) / 16));
   while (nchunk > 1 && ((std::min(ncol, nrow) % nchunk) || (nterms + 2) * nchunk > 1024)) nchunk >>= 1;
   void* args[] = {&z, &wpart, &nparts, &abs2, &nb2, &tv, &counter, &hist_row, &inv, &stop, &stop_on_purity, &t,
-                  &ncol, &nrow, &dX, &dP, &dXdP, &ts, &tk, &ti, &tc, &nterms, &nslots, &nchunk, &prm, &np, &hstride};
+                  &ncol, &nrow, &dX, &dP, &dXdP, &ts, &tk, &ti, &tc, &nterms, &nslots, &nchunk, &prm, &np, &hstride,
+                  &tptr};
   return hjit_on(h, h->k_final_rot, dim3((nterms + 2) * nchunk, h->vc), dim3(128), args, st ? st : h->st);
 }
 
@@ -1844,7 +2029,25 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
     a.stop = stop;
     TRY(row_pass(h, a, h->tw_r));
   }
-  for (long long n = 1; n <= steps; ++n) {
+  // Graph windows (see aw_graph): GW consecutive steps captured once and replayed.  A window holds no
+  // per-step argument: its kick tables are rebuilt into slots 0..GW before every replay, its step
+  // times read from h->vtimes by the observable reduction, its history rows written to h->hwin and
+  // copied into place after the replay.
+  const long long GW = std::min<long long>(AW_GRAPH_MAX, (steps - 2) & ~1LL);
+  const bool graphable = defer && h->graph_on && !kdep && c.absx_mode != 2 && !p.keep_rho && !p.stop_on_purity &&
+                         h->ni == 1 && !h->prof_on && GW >= AW_GRAPH_MIN;
+  long long win_n0 = 0;        // first step of the window being captured (0: none)
+  if (graphable) {
+    TRY(dalloc(h->vtimes, (size_t)VSEQ * sizeof(double)));
+    TRY(dalloc(h->hwin, (size_t)AW_GRAPH_MAX * h->hist_cols * sizeof(double)));
+    // the call's step times, uploaded once (a copy from pageable memory waits for the stream); each
+    // window copies its own on the device
+    TRY(dalloc(h->ctimes, (size_t)(steps + 2) * sizeof(double)));
+    CK(cudaMemcpyAsync(h->ctimes.p, times.data(), (size_t)(steps + 2) * sizeof(double), cudaMemcpyHostToDevice,
+                       h->st));
+  }
+
+  auto one_step = [&](long long n) -> int {
     const bool last = n == steps;
     const int par = defer ? (int)(n & 1) : 0;
     // column pass: scale, ifft0, K-kick, fft0
@@ -1869,15 +2072,19 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       a.d2 = +1;
       a.stop = stop;
       a.lines_hint = h->tuned_col_lines;
+      a.tma = h->tuned_col_tma;
+      a.shape = h->tuned_col_shape;
       TRY(col_pass(h, a, h->tw_c));
     }
-    // the marginal pass and reduction of step n - 2 read this parity's branch output and sums
-    if (defer && n >= 3) CK(cudaStreamWaitEvent(h->st, h->ev_f[par], 0));
+    // the marginal pass and reduction of step n - 2 read this parity's branch output and sums (in a
+    // window being captured, the first two steps' predecessors finished before the window started)
+    if (defer && n >= 3 && (!win_n0 || n >= win_n0 + 2)) CK(cudaStreamWaitEvent(h->st, h->ev_f[par], 0));
     // row pass: ifft1, V-kick(t_n) [branch: Wigner transform] [next kick(t_{n+1}), fft1 | S]
     {
       AwPassArgs a = pnone(h);
       a.in = a.out = h->rho.p;
       a.d1 = -1;
+      a.shape = h->tuned_row_shape;
       TRY(vfactor(n, false, &a.f1));
       if (p.ehrenfest) {
         a.br_out = wbuf(n);
@@ -1913,13 +2120,15 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       a.lines_hint = h->z_lines;
       a.cluster = h->z_cluster;
       a.stop = stop;
-      double* hrow = hist + (size_t)(n - 1) * h->hist_cols;
+      double* hrow = win_n0 ? (double*)h->hwin.p + (size_t)(n - win_n0) * h->hist_cols
+                            : hist + (size_t)(n - 1) * h->hist_cols;
+      const double* tptr = win_n0 ? (const double*)h->vtimes.p + (n - win_n0) : nullptr;
       if (defer) {
         // after the row pass of step n, on the side stream: marginal pass, then the reduction
         CK(cudaEventRecord(h->ev_z[par], h->st));
         CK(cudaStreamWaitEvent(side, h->ev_z[par], 0));
         TRY(col_pass(h, a, h->tw_c, side));
-        TRY(launch_finalize_rot(h, times[n], hrow, 0, par, side));
+        TRY(launch_finalize_rot(h, times[n], hrow, 0, par, side, tptr));
         CK(cudaEventRecord(h->ev_f[par], side));
       } else {
         TRY(col_pass(h, a, h->tw_c));
@@ -1931,6 +2140,92 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
         WignerGrid g{h->W.p, h->nr, h->nc, &h->tw_r, &h->tw_c};
         TRY(wigner_passes(h, g, h->W.p, fnone(), false, false, true, true));
       }
+    }
+    return AW_OK;
+  };
+
+  // one window of GW steps from n0 (even, and the window ends before the last step): inputs
+  // refreshed on the stream, the graph of the window's branch-output parity captured on first use,
+  // then replayed
+  auto window = [&](long long n0) -> int {
+    // the side stream's reductions of the steps before the window are done before it starts
+    for (int k = 0; k < 2; ++k) CK(cudaStreamWaitEvent(h->st, h->ev_f[k], 0));
+    // times t_{n0} .. t_{n0 + GW + 1}: the window's steps and the kicks of their successors (so that no
+    // table is rebuilt inside the window)
+    CK(cudaMemcpyAsync(h->vtimes.p, (const double*)h->ctimes.p + n0, (size_t)(GW + 2) * sizeof(double),
+                       cudaMemcpyDeviceToDevice, h->st));
+    if (vdep) {
+      vs_n0 = n0;
+      vs_cnt = GW + 2;
+      const double half = 0.5 * c.dt;
+      TRY(build_tab(h, 0, 0, 0, half, 0.0, -half, 0.0, 0.0, 0, 0.0, h->vseq.p, (const double*)h->vtimes.p,
+                    (int)vs_cnt));
+      TRY(fold_maskx(h, h->vseq.p, (int)vs_cnt));
+    }
+    // the graph of this window length and of this parity of the call's step count (which of W / tmp
+    // each step branches into)
+    const long long gkey = 2 * GW + (steps & 1);
+    int key = -1;
+    for (int k = 0; k < AW_GRAPH_CACHE; ++k)
+      if (h->graph_exec[k] && h->graph_key[k] == gkey) key = k;
+    if (key < 0) {
+      key = 0;  // a free slot, else the least recently used
+      for (int k = 0; k < AW_GRAPH_CACHE; ++k) {
+        if (!h->graph_exec[k]) {
+          key = k;
+          break;
+        }
+        if (h->graph_used[k] < h->graph_used[key]) key = k;
+      }
+      if (h->graph_exec[key]) {
+        cudaGraphExecDestroy(h->graph_exec[key]);
+        h->graph_exec[key] = nullptr;
+      }
+      h->graph_key[key] = gkey;
+      win_n0 = n0;
+      const long long launches0 = g_launches.load();
+      CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+      int r = AW_OK;
+      for (long long n = n0; n < n0 + GW && r == AW_OK; ++n) r = one_step(n);
+      // the side stream's last two reductions join the window
+      for (int k = 0; k < 2 && r == AW_OK; ++k)
+        if (cudaStreamWaitEvent(h->st, h->ev_f[k], 0) != cudaSuccess) r = fail(AW_E_CUDA, "graph join failed");
+      cudaGraph_t g = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(h->st, &g);
+      win_n0 = 0;
+      const long long captured = g_launches.load() - launches0;
+      g_launches = launches0;  // nothing ran during the capture: the launches count when the graph runs
+      cudaError_t ie = cudaErrorUnknown;
+      if (r == AW_OK && e == cudaSuccess) ie = cudaGraphInstantiate(&h->graph_exec[key], g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (ie != cudaSuccess) {
+        // nothing of the window ran: this handle steps on the streams from now on, starting here
+        h->graph_exec[key] = nullptr;
+        h->graph_on = false;
+        cudaGetLastError();
+        for (long long n = n0; n < n0 + GW; ++n) TRY(one_step(n));
+        return AW_OK;
+      }
+      h->graph_launches[key] = captured;
+    }
+    h->graph_used[key] = ++h->graph_clock;
+    CK(cudaGraphLaunch(h->graph_exec[key], h->st));
+    g_launches += h->graph_launches[key];
+    // the window's history rows, and the side-stream events re-recorded on the stream (their records
+    // inside the capture belong to the graph)
+    CK(cudaMemcpyAsync(hist + (size_t)(n0 - 1) * h->hist_cols, h->hwin.p, (size_t)GW * h->hist_cols * sizeof(double),
+                       cudaMemcpyDeviceToDevice, h->st));
+    for (int k = 0; k < 2; ++k) CK(cudaEventRecord(h->ev_f[k], h->st));
+    return AW_OK;
+  };
+
+  for (long long n = 1; n <= steps;) {
+    if (graphable && n >= 2 && !(n & 1) && n + GW <= steps) {
+      TRY(window(n));
+      n += GW;
+    } else {
+      TRY(one_step(n));
+      ++n;
     }
   }
   // join: the last reduction wrote the history and 1/norm that the caller applies
@@ -1997,7 +2292,7 @@ extern "C" int aw_history_of(aw_handle h, int32_t inst, double* out, int64_t max
     CK(cudaMemcpyAsync(out, hist_of(h, inst), (size_t)n * h->hist_cols * 8, cudaMemcpyDeviceToHost, h->st));
   }
   CK(cudaStreamSynchronize(h->st));
-  return AW_OK;
+  return check_err(h);
 }
 
 extern "C" int aw_history(aw_handle h, double* out, int64_t max_rows, int64_t* rows, int32_t* cols) {
@@ -2243,6 +2538,8 @@ static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::ve
       a.d2 = +1;
       a.stop = stop;
       a.lines_hint = h->tuned_col_lines;
+      a.tma = h->tuned_col_tma;
+      a.shape = h->tuned_col_shape;
       TRY(col_pass(h, a, h->tw_c));
     }
     {
@@ -2255,6 +2552,7 @@ static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::ve
       AwPassArgs a = pnone(h);
       a.in = a.out = h->rho.p;
       a.d1 = -1;
+      a.shape = h->tuned_row_shape;
       a.f1 = ftab(h, vslot);
       a.diag_out = (double2*)h->diag.p;
       if (p.stop_on_purity || p.bloch) a.red_abs2 = (double*)h->abs2.p;

@@ -323,12 +323,15 @@ extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw
 extern "C" __global__ void aw_finalize_rot(const double2* aw_z, const double2* aw_wpart, int aw_nparts,
                                            const double* aw_abs2, int aw_nb2, double* aw_tv, unsigned int* aw_counter,
                                            double* aw_hist, double* aw_inv_norm, int* aw_stop, int aw_stop_on_purity,
-                                           double t, int aw_ncol, int aw_nrow, double aw_dX, double aw_dP,
+                                           double aw_t_arg, int aw_ncol, int aw_nrow, double aw_dX, double aw_dP,
                                            double aw_dXdP, const int* aw_tslot, const int* aw_tkind,
                                            const int* aw_tidx, const double* aw_tcoef, int aw_nterms, int aw_nslots,
-                                           int aw_nchunk, const double* aw_params, int aw_np, long long aw_hstride) {
+                                           int aw_nchunk, const double* aw_params, int aw_np, long long aw_hstride,
+                                           const double* aw_tptr) {
   // blocks: (term or norm or purity) x chunk; FP64 expression evaluation spread over the GPU.
   // blockIdx.y = instance of a batch, with its own marginals, partials, history row and scalars.
+  // The observables' time: the argument, or (a step loop replayed from a CUDA graph) read from aw_tptr.
+  const double t = aw_tptr ? *aw_tptr : aw_t_arg;
   __shared__ double aw_red[256];
   __shared__ double aw_wg[256];
   __shared__ double aw_fsum[66];

@@ -7,6 +7,7 @@
 // and reduction of its program, and writes it once.
 #pragma once
 #include <cooperative_groups.h>
+#include <cudaTypedefs.h>
 
 #include <atomic>
 #include <type_traits>
@@ -14,6 +15,7 @@
 #include "aw_common.cuh"
 #include "aw_fft.cuh"
 #include "aw_pass.h"
+#include "aw_tma.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -27,14 +29,23 @@ namespace cg = cooperative_groups;
 // registers, 4 blocks a SM): more warps for the latency-bound row pass, whose branch point keeps a
 // second copy of the elements in registers (measured: 0.174 -> 0.170 ms a step; tiles of several
 // shorter rows spill at 64 registers and keep 8 elements a thread).
-template <typename V, int N, int LINES, bool ROW = false> struct Shape {
+// ALT: the other number of elements a thread (4 where the rule above gives 8, 8 where it gives 4), so
+// the other FFT radix (stages of radix min(8, E)); offered to the autotuner for lines of 256 to 2048
+// points where the block stays within 512 threads (ALT_OK).
+template <typename V, int N, int LINES, bool ROW = false, bool ALT = false> struct Shape {
   static constexpr int TILE = N * LINES;
-  static constexpr int E = (ROW && std::is_same<V, dfc>::value && N == 1024 && LINES == 1) ? 4
-                                                                                 : (TILE / 512 > 8 ? TILE / 512 : 8);
+  static constexpr int E0 = (ROW && std::is_same<V, dfc>::value && N == 1024 && LINES == 1) ? 4
+                                                                                  : (TILE / 512 > 8 ? TILE / 512 : 8);
+  static constexpr int E1 = E0 == 4 ? 8 : (E0 == 8 ? 4 : E0);
+  static constexpr bool ALT_OK = N >= 256 && N <= 2048 && E1 != E0 && TILE / E1 <= 512 && TILE % E1 == 0;
+  static constexpr int E = ALT ? E1 : E0;
   static constexpr int NT = TILE / E;
   // the tile fits the 128 KB a block is given: rows are padded by one element when LINES > 1
   static constexpr bool FITS_ROW = (LINES > 1 ? (N + 1) * LINES : N) * (int)sizeof(V) <= 128 * 1024;
-  static constexpr bool FITS_COL = N * LINES * (int)sizeof(V) <= 128 * 1024 && (N * LINES <= 4096 || LINES == 1);
+  // column tiles above 4096 elements keep 16 (complex64: 8-byte) elements a thread; the 16-byte types
+  // hold a single column there
+  static constexpr bool FITS_COL = N * LINES * (int)sizeof(V) <= 128 * 1024 &&
+                                   (N * LINES <= 4096 || LINES == 1 || (sizeof(V) == 8 && N * LINES <= 8192));
 };
 
 template <typename V> struct RealOf;
@@ -163,11 +174,14 @@ __device__ __forceinline__ double block_sum(double x, double* red, int tid) {
 // REDUCE_ONLY: the reduction-only column pass (load, FFT d1, f1, column reductions, nothing stored),
 // compiled without the segment loop so that its code is a fraction of the full pass's; it needs
 // fewer registers and runs 3 blocks of 256 threads a SM (0.1555 -> 0.1537 ms a step).
-template <typename V, class Tile, int NT, bool REDUCE_ONLY = false>
+// TMA: (column tiles) the tile arrives in shared memory by tensor copies and `out` leaves it the same
+// way (aw_tma.cuh); everything between is the register-resident program of the direct form, so the
+// two forms give bit-identical results.
+template <typename V, class Tile, int NT, bool REDUCE_ONLY = false, bool TMA = false>
 __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 1)
                                                               : (NT <= 128 ? 5 : (NT <= 256 ? (REDUCE_ONLY ? 3 : 2) : 1))))
     aw_pass_kernel(const __grid_constant__ AwPassArgs a) {
-  extern __shared__ __align__(16) unsigned char aw_smem[];
+  extern __shared__ __align__(128) unsigned char aw_smem[];
   typedef typename RealOf<V>::type T;
   V* s = reinterpret_cast<V*>(aw_smem);
   constexpr int L = Tile::LINES;
@@ -187,9 +201,44 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
   const V* in = (const V*)a.in + eoff;
   const V* tw = (const V*)a.tw;
 
+  // TMA geometry: 8-byte words per element, rows per box, boxes per tile; tensor row of this
+  // instance's row 0 (the instances of the launch are stacked rows of one tensor)
+  constexpr int TW = sizeof(V) / 8;
+  constexpr int TR = Tile::N < 256 ? Tile::N : 256;
+  constexpr int TBOX = Tile::N / TR;
+  const int ty0 = a.batch_elems ? inst * a.nrows : 0;
+
   V r[E];
+  if constexpr (TMA && !Tile::IS_ROW) {
+    __shared__ __align__(8) uint64_t tma_bar;
+    // box destinations must be 128-byte aligned: a block whose tile is not records it and copies nothing
+    if (aw_smem_addr(s) & 127) {
+      if (tid == 0 && a.err) atomicExch(a.err, AW_TMA_MISALIGNED);
+      return;
+    }
+    if (tid == 0) {
+      aw_mbar_init(&tma_bar, 1);
+      aw_fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      aw_mbar_arrive_expect_tx(&tma_bar, (uint32_t)(sizeof(V) * Tile::SMEM_ELEMS));
+#pragma unroll 1
+      for (int b = 0; b < TBOX; ++b) aw_tma_load_2d(s + b * TR * L, a.tmap_in, line0 * TW, ty0 + b * TR, &tma_bar);
+    }
+    if (!__syncthreads_and(aw_mbar_wait(&tma_bar, 0))) {
+      // the copies did not arrive in time: record it, give them a second bounded wait (they write into
+      // this block's shared memory) and leave
+      if (tid == 0 && a.err) atomicExch(a.err, AW_TMA_TIMEOUT);
+      aw_mbar_wait(&tma_bar, 0);
+      return;
+    }
 #pragma unroll
-  for (int k = 0; k < E; ++k) r[k] = in[gidx<Tile>(lg, pos0 + k * STEP, ncols)];
+    for (int k = 0; k < E; ++k) r[k] = s[Tile::addr(line, pos0 + k * STEP)];
+  } else {
+#pragma unroll
+    for (int k = 0; k < E; ++k) r[k] = in[gidx<Tile>(lg, pos0 + k * STEP, ncols)];
+  }
 
   if constexpr (REDUCE_ONLY) {
     run_fft<Tile, NT>(r, s, tw, a.d1, tid);
@@ -237,7 +286,23 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
       for (int k = 0; k < E; ++k) r[k] = keep[k];
     }
   }
-  if (a.out) store_regs<V, Tile, NT>((V*)a.out + eoff, r, lg, pos0, ncols, false);
+  if (a.out) {
+    if constexpr (TMA && !Tile::IS_ROW) {
+      __syncthreads();  // every thread has read the tile's last FFT stage
+#pragma unroll
+      for (int k = 0; k < E; ++k) s[Tile::addr(line, pos0 + k * STEP)] = r[k];
+      aw_fence_proxy_async_smem();
+      __syncthreads();
+      if (tid == 0) {
+#pragma unroll 1
+        for (int b = 0; b < TBOX; ++b) aw_tma_store_2d(a.tmap_out, line0 * TW, ty0 + b * TR, s + b * TR * L);
+        aw_bulk_commit();
+        aw_bulk_wait_read();  // the block's shared memory stays until the copies have read it
+      }
+    } else {
+      store_regs<V, Tile, NT>((V*)a.out + eoff, r, lg, pos0, ncols, false);
+    }
+  }
   if (a.red_abs2 && a.abs2_end) {
     T acc = from_double<T>(0.0);
 #pragma unroll
@@ -377,7 +442,8 @@ inline int choose_row_lines(int nrows, int ncols, int esz) {
 // threads so that the 16-byte element types keep their registers)
 inline int max_col_lines(int nrows, int ncols, int esz) {
   int b = 16;
-  while (b > 1 && ((long long)nrows * b * esz > 128 * 1024 || (long long)nrows * b > 4096 || ncols % b))
+  const long long most = esz == 8 ? 8192 : 4096;  // elements of a tile (Shape::FITS_COL)
+  while (b > 1 && ((long long)nrows * b * esz > 128 * 1024 || (long long)nrows * b > most || ncols % b))
     b >>= 1;
   return b;
 }
@@ -408,11 +474,11 @@ static int prepare_smem(K kern, size_t max_dynamic, std::atomic<int>* slots) {
   return (int)want;
 }
 
-template <typename V, int N, int LINES>
+template <typename V, int N, int LINES, bool ALT = false>
 static int launch_row_t(const AwPassArgs* a, int batch, cudaStream_t st) {
-  typedef Shape<V, N, LINES, true> S;
-  if constexpr (!S::FITS_ROW) {
-    return -5;
+  typedef Shape<V, N, LINES, true, ALT> S;
+  if constexpr (!S::FITS_ROW || (ALT && !S::ALT_OK)) {
+    return ALT ? -9 : -5;
   } else {
     typedef RowTile<N, LINES> Tile;
     if (a->nrows % LINES) return -2;
@@ -426,15 +492,83 @@ static int launch_row_t(const AwPassArgs* a, int batch, cudaStream_t st) {
   }
 }
 
-template <typename V, int N, int LINES>
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+static PFN_cuTensorMapEncodeTiled_v12000 aw_encode_tiled() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    return (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }();
+  return fn;
+}
+
+// Tensor map of a column slab source or destination: `rows` rows (every instance of the launch,
+// stacked) of ncols elements of esz bytes, seen as 8-byte words; boxes of `lines` columns by `box_rows`
+// rows.  0 on success.
+static int aw_column_tmap(void* map, const void* base, int ncols, long long rows, int esz, int lines, int box_rows) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = aw_encode_tiled();
+  if (!enc) return -8;
+  const cuuint64_t dim[2] = {(cuuint64_t)ncols * (esz / 8), (cuuint64_t)rows};
+  const cuuint64_t stride[1] = {(cuuint64_t)ncols * esz};
+  const cuuint32_t box[2] = {(cuuint32_t)(lines * esz / 8), (cuuint32_t)box_rows};
+  const cuuint32_t es[2] = {1, 1};
+  const CUresult r = enc((CUtensorMap*)map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<void*>(base), dim, stride,
+                         box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 0 : -8;
+}
+
+// whether a column pass of LINES columns of V can be staged by TMA: every box row a multiple of 16
+// bytes (so that each box starts on a 16-byte boundary), contiguous instances, 16-byte aligned
+// buffers, one store target
+template <typename V, int LINES>
+static bool col_tma_ok(const AwPassArgs* a) {
+  if ((LINES * (int)sizeof(V)) % 16 || !a->out || a->mid_out || a->br_out) return false;
+  if (a->batch_elems != 0 && a->batch_elems != (long long)a->nrows * a->ncols) return false;
+  if (((uintptr_t)a->in | (uintptr_t)a->out) & 15) return false;
+  return true;
+}
+
+template <typename V, int N, int LINES, bool ALT = false>
 static int launch_col_t(const AwPassArgs* a, int batch, cudaStream_t st) {
-  typedef Shape<V, N, LINES> S;
-  if constexpr (!S::FITS_COL) {
-    return -5;
+  typedef Shape<V, N, LINES, false, ALT> S;
+  if constexpr (!S::FITS_COL || (ALT && !S::ALT_OK)) {
+    return ALT ? -9 : -5;
   } else {
+    // the other shape serves the storing passes only (the reduction-only and clustered passes keep
+    // the rule's)
+    if (ALT && (!a->out || (a->alt_cross && a->cluster > 1))) return -9;
     typedef ColTile<N, LINES> Tile;
     if (a->ncols % LINES) return -2;
     const bool clustered = a->alt_cross && a->cluster > 1;
+    if (a->tma && !clustered && col_tma_ok<V, LINES>(a)) {
+      // TMA-staged form of the pass (its program has no cluster reductions)
+      AwPassArgs b = *a;
+      const long long rows = a->batch_elems ? (long long)(a->inst0 + batch) * N : (long long)N;
+      constexpr int R = N < 256 ? N : 256;
+      if (aw_column_tmap(b.tmap_in, a->in, a->ncols, rows, (int)sizeof(V), LINES, R) ||
+          aw_column_tmap(b.tmap_out, a->out, a->ncols, rows, (int)sizeof(V), LINES, R))
+        return -8;
+      const size_t smem = sizeof(V) * Tile::SMEM_ELEMS;
+      auto kern = aw_pass_kernel<V, Tile, S::NT, false, true>;
+      static std::atomic<int> granted_t[AW_MAX_DEVICES];
+      if (prepare_smem(kern, smem, granted_t) < (int)smem) return -3;
+      dim3 grid(a->ncols / LINES, batch);
+      kern<<<grid, S::NT, smem, st>>>(b);
+      return cudaGetLastError() == cudaSuccess ? 0 : -4;
+    }
+    if constexpr (ALT) {
+      // the other shape: plain storing passes, unclustered
+      const size_t smem = sizeof(V) * Tile::SMEM_ELEMS;
+      auto kern = aw_pass_kernel<V, Tile, S::NT, false>;
+      static std::atomic<int> granted_a[AW_MAX_DEVICES];
+      if (prepare_smem(kern, smem, granted_a) < (int)smem) return -3;
+      kern<<<dim3(a->ncols / LINES, batch), S::NT, smem, st>>>(*a);
+      return cudaGetLastError() == cudaSuccess ? 0 : -4;
+    } else {
     // a clustered launch keeps one row of partials (N complex FP64) behind the tile
     const size_t smem = sizeof(V) * Tile::SMEM_ELEMS + (clustered ? sizeof(double2) * N : 0);
     const bool reduce_only = !a->out && !a->mid_out && !a->br_out && !a->f0.active && !a->d2 && !a->f2.active &&
@@ -465,27 +599,36 @@ static int launch_col_t(const AwPassArgs* a, int batch, cudaStream_t st) {
     cfg.numAttrs = 1;
     cudaError_t e = cudaLaunchKernelEx(&cfg, kern, *a);
     return e == cudaSuccess ? 0 : -4;
+    }
   }
 }
 
-template <typename V, int N> static int launch_row_n(const AwPassArgs* a, int batch, cudaStream_t st) {
+template <typename V, int N, bool ALT> static int launch_row_s(const AwPassArgs* a, int batch, cudaStream_t st) {
   constexpr int L = 1024 / N >= 1 ? 1024 / N : 1;
   const int l = a->row_lines ? a->row_lines : choose_row_lines(a->nrows, N, (int)sizeof(V));
   if constexpr (L > 1) {
-    if (l == 1) return launch_row_t<V, N, 1>(a, batch, st);
+    if (l == 1) return launch_row_t<V, N, 1, ALT>(a, batch, st);
   }
-  return l == L ? launch_row_t<V, N, L>(a, batch, st) : -7;
+  return l == L ? launch_row_t<V, N, L, ALT>(a, batch, st) : -7;
+}
+
+template <typename V, int N> static int launch_row_n(const AwPassArgs* a, int batch, cudaStream_t st) {
+  return a->shape ? launch_row_s<V, N, true>(a, batch, st) : launch_row_s<V, N, false>(a, batch, st);
+}
+
+template <typename V, int N, bool ALT> static int launch_col_s(const AwPassArgs* a, int batch, cudaStream_t st) {
+  switch (a->lines_hint ? a->lines_hint : choose_col_lines(a->nrows, a->ncols, batch, (int)sizeof(V))) {
+    case 1: return launch_col_t<V, N, 1, ALT>(a, batch, st);
+    case 2: return launch_col_t<V, N, 2, ALT>(a, batch, st);
+    case 4: return launch_col_t<V, N, 4, ALT>(a, batch, st);
+    case 8: return launch_col_t<V, N, 8, ALT>(a, batch, st);
+    case 16: return launch_col_t<V, N, 16, ALT>(a, batch, st);
+    default: return -1;
+  }
 }
 
 template <typename V, int N> static int launch_col_n(const AwPassArgs* a, int batch, cudaStream_t st) {
-  switch (a->lines_hint ? a->lines_hint : choose_col_lines(a->nrows, a->ncols, batch, (int)sizeof(V))) {
-    case 1: return launch_col_t<V, N, 1>(a, batch, st);
-    case 2: return launch_col_t<V, N, 2>(a, batch, st);
-    case 4: return launch_col_t<V, N, 4>(a, batch, st);
-    case 8: return launch_col_t<V, N, 8>(a, batch, st);
-    case 16: return launch_col_t<V, N, 16>(a, batch, st);
-    default: return -1;
-  }
+  return a->shape ? launch_col_s<V, N, true>(a, batch, st) : launch_col_s<V, N, false>(a, batch, st);
 }
 
 #define AW_FOR_SIZES(M) M(32) M(64) M(128) M(256) M(512) M(1024) M(2048) M(4096) M(8192)

@@ -70,6 +70,13 @@ typedef struct AwPassArgs {
   long long batch_tab;      // ... table entries per instance
   int inst0;                // instance of blockIdx.y = 0 (a launch over a range of a batch's instances)
   int row_lines;            // row pass: rows per block (0: chosen from nrows)
+  int tma;                  // column pass: stage the tile load and the store of `out` by TMA (tensor maps
+                            // filled in by the launcher)
+  int* err;                 // device error word: a bounded wait that ran out records its code here (or 0)
+  int shape;                // 0: elements a thread (and so FFT radix) by the size rule; 1: the other choice
+                            // (launchers return -9 where it does not exist)
+  alignas(64) unsigned char tmap_in[128];   // CUtensorMap of `in`, then of `out` (launcher-written)
+  alignas(64) unsigned char tmap_out[128];
 } AwPassArgs;
 
 // Host-side launchers, one per precision (aw_pass_f64.cu / aw_pass_f32.cu).

@@ -720,14 +720,10 @@ def run_frames(args):
            "clocks": clk.summary()})
 
 
-def run_large_vn(args):
-    """von Neumann 4096 x 4096, X_amplitude = 80, Morse V = D (1 - exp(-alpha (x - x0)))^2 + x 0.02 sin(0.01 t)
-    (D = 0.18, alpha = 1, x0 = 1.4), dt = 0.02, 2000 steps; rho0 = sum of 8 seeded Gaussian pure states."""
-    from accuratewigner_gb300 import RhoVNeumannCUDA1D
-
-    n, steps = 4096, args.steps if args.steps != 200 else 2000
-    # the Morse wall capped at 1e4 (it reaches 9e69 at x = -80, where kick phases would depend on the
-    # last bits of V); states in the well move as under the uncapped wall
+def large_vn_config(n=4096):
+    """Parameters and initial state of the 4096^2 von Neumann workload.  The Morse wall is capped at 1e4
+    (it reaches 9e69 at x = -80, where kick phases would depend on the last bits of V); states in the
+    well move as under the uncapped wall."""
     morse = "D * pow(1. - exp(-alpha * (X - xm)), 2)"
     p = dict(t=0.0, dt=0.02, X_gridDIM=n, X_amplitude=80.0, D=0.18, alpha=1.0, xm=1.4, Vcap=1e4, K="0.5 * P * P",
              V="fmin(%s, Vcap) + X * 0.02 * sin(0.01 * t)" % morse, diff_K="P",
@@ -746,6 +742,17 @@ def run_large_vn(args):
             r += wk * np.outer(g, g)
         return r
 
+    return p, rho0
+
+
+def run_large_vn(args):
+    """von Neumann 4096 x 4096, X_amplitude = 80, Morse V = D (1 - exp(-alpha (x - x0)))^2 + x 0.02 sin(0.01 t)
+    (D = 0.18, alpha = 1, x0 = 1.4), dt = 0.02, 2000 steps; rho0 = sum of 8 seeded Gaussian pure states."""
+    from accuratewigner_gb300 import RhoVNeumannCUDA1D
+
+    n, steps = 4096, args.steps if args.steps != 200 else 2000
+    p, rho0 = large_vn_config()
+
     def run(prec, k):
         g = RhoVNeumannCUDA1D(precision=prec, **p)
         g.set_rho(rho0())
@@ -761,14 +768,44 @@ def run_large_vn(args):
     extra = {"ms_per_step": sec / steps * 1e3, "achieved_gbs": bytes_per_pt * n * n * steps / sec / 1e9,
              "algorithmic_bytes_per_pt_step": bytes_per_pt, "trace": float(np.trace(rho).real * 160.0 / n),
              "purity": float(pur), "x_final": float(xav[-1]), "clocks": clk.summary()}
-    if args.precision != "c128":
-        _, rref, xref, pref = run("c128", steps)
-        extra["vs_c128"] = {"rho_rel_l2": float(np.linalg.norm(rho - rref) / np.linalg.norm(rref)),
-                            "x_max_abs_err": float(np.max(np.abs(xav - xref))), "purity_err": float(abs(pur - pref))}
+    if args.precision != "c128-fp64":
+        # against the native FP64 form (held to the FP64 oracle at 1e-10 by the 4096^2 parity test)
+        _, rref, xref, pref = run("c128-fp64", steps)
+        tr = float(np.trace(rho).real * 160.0 / n)
+        tref = float(np.trace(rref).real * 160.0 / n)
+        extra["vs_fp64"] = {"rho_rel_l2": float(np.linalg.norm(rho - rref) / np.linalg.norm(rref)),
+                            "trace_err": abs(tr - tref), "purity_err": float(abs(pur - pref)),
+                            "x_max_abs_err": float(np.max(np.abs(xav - xref)))}
     _line("large-vn", "grid-pt*steps/s", n * n * steps / sec, "grid-pt*steps/s", sec, args,
           {"grid": [n, n], "X_amplitude": 80.0, "dt": 0.02, "steps": steps, "potential": "Morse capped at 1e4",
            "initial": "8 Gaussians, centres U(0.5, 4), seed 0",
            "precision": args.precision}, extra)
+
+
+def run_profile_window(args):
+    """The headline (or the 4096^2 von Neumann) workload with `--profile-steps` steps inside a profiler
+    range: the launches an ncu capture with --profile-from-start off sees are those steps' alone."""
+    import torch
+
+    torch.cuda.init()
+    if args.workload == "large-vn":
+        from accuratewigner_gb300 import RhoVNeumannCUDA1D
+
+        p, rho0 = large_vn_config()
+        g = RhoVNeumannCUDA1D(precision=args.precision, **p)
+        g.set_rho(rho0())
+    else:
+        g = make_propagator(args.precision)
+    g.propagate(max(args.warmup, 3))
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    t0 = time.perf_counter()
+    g.propagate(args.profile_steps)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print(json.dumps({"profile_window": args.workload, "precision": args.precision, "steps": args.profile_steps,
+                      "ms_per_step": (time.perf_counter() - t0) / args.profile_steps * 1e3}))
+    g.close()
 
 
 def main():
@@ -780,6 +817,9 @@ def main():
     ap.add_argument("--precision", default="c128-fp64", choices=["c128", "c128-fp64", "c64", "auto"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="headline: skip the other arithmetic forms")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="set up the workload (headline or large-vn), warm up, run this many steps inside a "
+                         "cudaProfilerStart/Stop range (for ncu --profile-from-start off) and exit")
     ap.add_argument("--workload", default="strong-field",
                     choices=["strong-field", "plain", "batched-gibbs", "served", "served-sweep", "large-vn",
                              "precision", "frames"])
@@ -794,6 +834,9 @@ def main():
              "frames": run_frames}
     if args.precision == "auto" and args.workload not in ("served", "served-sweep"):
         ap.error("--precision auto chooses per request: only the served workload has requests")
+    if args.profile_steps:
+        run_profile_window(args)
+        return
     if args.workload in other:
         import torch
 

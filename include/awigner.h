@@ -142,6 +142,33 @@ int64_t aw_launch_count(void);
  * passes, 1 column passes that store, 2 expression kernels, 3 helper kernels,
  * 4 reduction-only column passes), the summed device time in ms, the summed
  * algorithmic HBM bytes and the launch count: arrays of AW_PROF_CLASSES. */
+/* Forms of the propagation passes (no counterpart in the reference; its axis-0
+ * and axis-1 cuFFT plans, cufft.py:274-343, leave no such choice), as chosen by
+ * the autotuner when the handle is created: form[0] columns per column-pass
+ * block, form[1] whether the column tile is staged in shared memory by TMA
+ * tensor copies instead of per-thread loads, form[2] elements a thread (and so
+ * the FFT radix) of the column pass, 0 by the size rule or 1 the other choice,
+ * form[3] the same for the row pass.  The column forms are timed per handle and
+ * never change a result; the row shape is timed once per grid and form in the
+ * process (the purity sum over row blocks follows it).  `set` (4 entries, < 0
+ * keeps an entry; may be null) overrides, `get` (may be null) receives the
+ * forms in force.  Columns per block: a power of two dividing the columns; TMA
+ * needs rows of a multiple of 16 bytes. */
+int aw_pass_form(aw_handle h, const int32_t* set, int32_t* get);
+
+/* CUDA graphs of the Wigner-Moyal step loop (no counterpart in the reference,
+ * whose propagate() launches every kernel from a Python loop,
+ * wigner_moyal_cuda_1d.py:563-582).  With Ehrenfest observables, aw_propagate
+ * runs windows of its steps (as many as fit, 16 to 248, an even count) from a
+ * graph captured on first use per window length and replayed (the kick tables,
+ * step times and history rows of a window live at fixed device addresses,
+ * refreshed on the stream between windows); the first step, the last and any
+ * remainder run on the streams.  Results are bit-identical with and without
+ * graphs.  On by default for grids of at most 512 x 512 points, where launch
+ * latency is a large part of a step; enable = 0 turns it off for the handle, 1
+ * on. */
+int aw_graph(aw_handle h, int32_t enable);
+
 #define AW_PROF_CLASSES 5
 int aw_profile(aw_handle h, int32_t enable);
 int aw_profile_read(aw_handle h, double* ms, double* bytes, int64_t* launches);
