@@ -180,6 +180,8 @@ struct aw_state_s {
   long long graph_launches[AW_GRAPH_CACHE] = {};
   long long graph_clock = 0;
   DevBuf hwin;                         // history rows of one window
+  // native FP64: tangent-form twiddle tables (aw_fft.cuh) of the lengths of tw_r, tw_c, tw_w, tw_l1, tw_l2
+  DevBuf tt_r[2], tt_c[2], tt_w[2], tt_l1[2], tt_l2[2];
   DevBuf ctimes;                       // step times of the current call
   int* err_dev = nullptr;              // ... its device address
   cudaKernel_t k_binit = nullptr;
@@ -199,6 +201,9 @@ struct aw_state_s {
   DevBuf rho, W, snap, tmp, stage;
   DevBuf tw_r, tw_c, tw_w;            // twiddles: row length (nc), column length (nr), Wigner grid (wn)
   DevBuf shx_hi, shx_lo, shy_hi, shy_lo;
+  // native FP64 on grids up to 1024 x 1024: the shear factors of the per-step Wigner transform as full
+  // [lines][positions] tables (one complex product a point fewer on the FP64 pipe)
+  DevBuf shx_full, shy_full;
   DevBuf tabs;                         // phase tables, slots of (nc + nr) complex
   DevBuf vseq, vtimes;                 // time-dependent kick tables of a run of time points, their times
   DevBuf maskx, maskp;                 // 2-D masks (rotated frame)
@@ -418,6 +423,62 @@ static int upload_reals(DevBuf& dst, const std::vector<double>& v, int fmt) {
 }
 
 // twiddle table tw[m] = exp(-2 pi i m / n), built in extended precision
+// Tangent-form twiddle table of length n for the native FP64 passes (layout: aw_fft.cuh, tan_off):
+// for R in {2, 4, 8}, NS = 1 .. n / 2, k < NS, the entries of w = exp(-2 pi i k / (NS R)) listed there,
+// each as t = i^e m (1 + i q) with |q| <= 1, computed in extended precision.
+static int make_tan_twiddles(DevBuf* tt, int n) {
+  const long double PI = 3.141592653589793238462643383279502884L;
+  const size_t count = (size_t)7 * (n - 1);
+  std::vector<double> mq(2 * count);
+  std::vector<unsigned char> ee(count);
+  size_t at = 0;
+  for (int ri = 0; ri < 3; ++ri) {
+    const int R = 2 << ri;
+    for (long long ns = 1; ns < n; ns *= 2)
+      for (long long k = 0; k < ns; ++k) {
+        const long double base = (long double)k / (long double)(ns * R);  // w = exp(-2 pi i base)
+        long double f[4];
+        int nf = 0;
+        if (R == 8) {
+          f[nf++] = 4 * base;
+          f[nf++] = 2 * base;
+          f[nf++] = base;
+          f[nf++] = base + 0.125L;
+        } else if (R == 4) {
+          f[nf++] = 2 * base;
+          f[nf++] = base;
+        } else {
+          f[nf++] = base;
+        }
+        for (int j = 0; j < nf; ++j) {
+          const long double a = 2.0L * PI * f[j];
+          const long double c = cosl(a), sn = -sinl(a);
+          long double m, q;
+          int e;
+          if (fabsl(c) >= fabsl(sn)) {
+            m = c;
+            q = sn / c;
+            e = 0;
+          } else {  // c + i s = i s (1 - i c / s)
+            m = sn;
+            q = -c / sn;
+            e = 1;
+          }
+          mq[2 * at] = (double)m;
+          mq[2 * at + 1] = (double)q;
+          ee[at] = (unsigned char)e;
+          ++at;
+        }
+      }
+  }
+  if (at != count) return fail(AW_E_STATE, "tangent twiddle table: %zu entries for %zu", at, count);
+  TRY(dalloc(tt[0], mq.size() * sizeof(double)));
+  TRY(dalloc(tt[1], ee.size()));
+  TRY(h2d(tt[0].p, mq.data(), mq.size() * sizeof(double)));
+  TRY(h2d(tt[1].p, ee.data(), ee.size()));
+  return AW_OK;
+}
+
 static int make_twiddles(DevBuf& dst, int n, int fmt) {
   const long double PI = 3.141592653589793238462643383279502884L;
   std::vector<double> h(2 * (size_t)n);
@@ -614,6 +675,17 @@ static void df_outputs(aw_state_s* h, const AwPassArgs& a, int batch) {
 static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row, cudaStream_t st = nullptr) {
   if (!st) st = h->st;
   a.tw = tw.p;
+  if (!h->df && !h->f32) {
+    // the native FP64 passes take the tangent-form table of the same length
+    const DevBuf* tt = &tw == &h->tw_r ? h->tt_r
+                       : &tw == &h->tw_c ? h->tt_c
+                       : &tw == &h->tw_w ? h->tt_w
+                       : &tw == &h->tw_l1 ? h->tt_l1
+                       : &tw == &h->tw_l2 ? h->tt_l2 : nullptr;
+    if (!tt || !tt[0].p) return fail(AW_E_STATE, "no tangent twiddle table for this pass");
+    a.twt_mq = tt[0].p;
+    a.twt_e = (const unsigned char*)tt[1].p;
+  }
   const int batch = h->vc;
   if (h->ni > 1) {
     // every pass of a batch skips the instances that are stopped or inactive, and splits its
@@ -1157,13 +1229,22 @@ static int create_impl(const aw_config* cfg, aw_state_s* h, bool check_only = fa
   if (h->sw_n1) {
     TRY(make_twiddles(h->tw_l1, h->sw_n1, tab_fmt(h)));
     TRY(make_twiddles(h->tw_l2, h->sw_n2, tab_fmt(h)));
+    if (tab_fmt(h) == 0) {
+      TRY(make_tan_twiddles(h->tt_l1, h->sw_n1));
+      TRY(make_tan_twiddles(h->tt_l2, h->sw_n2));
+    }
     TRY(make_twist4(h->swf_hi, h->swf_lo, &h->swt_lo_n, h->sw_n2, h->sw_n1, N, -1, tab_fmt(h)));
     TRY(make_twist4(h->swi_hi, h->swi_lo, &h->swt_lo_n, h->sw_n2, h->sw_n1, N, +1, tab_fmt(h)));
   } else {
     TRY(make_twiddles(h->tw_r, h->nc, tab_fmt(h)));
+    if (tab_fmt(h) == 0) TRY(make_tan_twiddles(h->tt_r, h->nc));
   }
   if (!h->kn.sw) TRY(make_twiddles(h->tw_c, h->nr, tab_fmt(h)));
   if (h->wn) TRY(make_twiddles(h->tw_w, h->wn, tab_fmt(h)));
+  if (tab_fmt(h) == 0) {
+    if (!h->kn.sw) TRY(make_tan_twiddles(h->tt_c, h->nr));
+    if (h->wn) TRY(make_tan_twiddles(h->tt_w, h->wn));
+  }
 
   // shear tables of the Wigner transform
   const double a_shx = tan(M_PI / 8.0);   // phase_shearX: a = tan(theta / 2)
@@ -1176,6 +1257,13 @@ static int create_impl(const aw_config* cfg, aw_state_s* h, bool check_only = fa
     for (int j = 0; j < h->nc; ++j) ay[j] = -b_shy * cfg->dPP_prime * (cfg->dXX * ((double)j - 0.5 * h->nc));
     TRY(make_shear(h->shx_hi, h->shx_lo, &h->shx_lo_n, ax, h->nc, 1.0 / h->nc, tab_fmt(h)));
     TRY(make_shear(h->shy_hi, h->shy_lo, &h->shy_lo_n, ay, h->nr, 1.0 / h->nr, tab_fmt(h)));
+    if (tab_fmt(h) == 0 && (long long)h->nr * h->nc <= 1024LL * 1024) {
+      // X shear: nr lines (rows) of nc positions; Y shear: nc lines (columns) of nr positions
+      TRY(dalloc(h->shx_full, (size_t)h->nr * h->nc * 16));
+      TRY(dalloc(h->shy_full, (size_t)h->nr * h->nc * 16));
+      KL(aw_k_shear_full(h->shx_hi.p, h->shx_lo.p, h->shx_lo_n, h->nr, h->nc, h->shx_full.p, h->st));
+      KL(aw_k_shear_full(h->shy_hi.p, h->shy_lo.p, h->shy_lo_n, h->nc, h->nr, h->shy_full.p, h->st));
+    }
   } else if (h->kn.vn) {
     // rho_vneumann_cuda_1d.py:608-639 on the padded (2N)^2 grid, dXX = dX
     const int M = h->wn;
@@ -1283,7 +1371,9 @@ extern "C" int aw_destroy(aw_handle h) {
                     &h->shx_lo, &h->shy_hi, &h->shy_lo, &h->tabs, &h->maskx, &h->maskp, &h->red_line,
                     &h->red_cross, &h->red_sq, &h->rowsum, &h->diag, &h->abs2, &h->scal, &h->stop, &h->hist,
                     &h->terms, &h->part, &h->blk_tabs, &h->params, &h->bvec, &h->maskx2, &h->masksep,
-                    &h->hwin, &h->ctimes};
+                    &h->hwin, &h->ctimes, &h->tt_r[0], &h->tt_r[1], &h->tt_c[0], &h->tt_c[1], &h->tt_w[0],
+                    &h->tt_w[1], &h->tt_l1[0], &h->tt_l1[1], &h->tt_l2[0], &h->tt_l2[1], &h->shx_full,
+                    &h->shy_full};
   for (DevBuf* b : bufs) dfree(*b);
   for (DevBuf& b : h->sw_states) dfree(b);
   for (auto& g : h->graph_exec)
@@ -1514,6 +1604,7 @@ static AwFactor fshear_x(aw_state_s* h) {
   f.sh_hi = h->shx_hi.p;
   f.sh_lo = h->shx_lo.p;
   f.sh_lo_n = h->shx_lo_n;
+  f.sh_full = h->shx_full.p;
   f.active = 1;
   return f;
 }
@@ -1521,6 +1612,7 @@ static AwFactor fshear_y(aw_state_s* h) {
   AwFactor f = fnone();
   f.sh_hi = h->shy_hi.p;
   f.sh_lo = h->shy_lo.p;
+  f.sh_full = h->shy_full.p;
   f.sh_lo_n = h->shy_lo_n;
   f.active = 1;
   return f;
@@ -2061,6 +2153,12 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       a.f0.active = 1;
       a.d1 = -1;
       a.f1 = ftab(h, p.bloch ? TAB_BK : TAB_K);
+      if (!a.f0.scale_ptr) {
+        // 1/N^2 is a power of two: applied after ifft0, folded into the K kick's per-column constant,
+        // it gives the same bits and saves a complex product a point
+        a.f0 = fnone();
+        a.f1.scale = inv_n2;
+      }
       if (!p.bloch && c.absp_mode) {
         if (c.absp_mode == 2 || !h->maskp_ready) {
           TRY(build_mask2d(h, 1, times[n]));

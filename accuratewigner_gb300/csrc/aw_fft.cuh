@@ -23,6 +23,8 @@
 // (read all inputs, synchronise, write all outputs).  Element-wise factors,
 // global loads and stores and reductions all work on the registers.
 #pragma once
+#include <type_traits>
+
 #include "aw_common.cuh"
 
 // Tile geometry: a row tile holds L lines of N contiguous elements (padded by
@@ -108,6 +110,95 @@ template <typename V> struct Dft<8, V> {
   }
 };
 
+// ---------------------------------------------------------------- native FP64: tangent-form butterflies
+// The native FP64 passes are bound by the FP64 pipe, so their FFT is written to need the fewest FP64
+// instructions.  A radix-R stage with twiddle w = exp(-+2 pi i k / (NS R)) is computed as log2 R
+// levels of twiddled radix-2 butterflies (decimation in time on the stage's R inputs), each
+//   a, b  ->  a + t b, a - t b
+// with its twiddle in tangent form t = i^e m (1 + i q), |q| <= 1 (m = cos, q = tan when |cos| >= |sin|;
+// m = sin, q = -cot and e = 1 otherwise): u = b (1 + i q) is two FMAs, the factor i^e a swap and sign
+// flips on the integer pipe, and a +- m i^e u four FMAs: 6 FP64 instructions a butterfly where a
+// complex product and two complex sums take 8, and two roundings per output instead of three
+// (Linzer and Feig, "Implementation of efficient FFT algorithms on fused multiply-add
+// architectures", IEEE Trans. Signal Processing 41, 1993).  A 1024-point transform of radix-8, 8, 8,
+// 2 stages needs 27.5 FP64 instructions a point instead of 32.  The first stage (w = 1) keeps the
+// plain radix kernels.
+//
+// Table (built on the host in extended precision, one per line length N): for R in {2, 4, 8}, span
+// NS in {1, 2, .., N / 2} and k < NS, the entries of w = exp(-2 pi i k / (NS R)):
+//   R = 8: w^4, w^2, w, w W8     R = 4: w^2, w     R = 2: w          (W8 = exp(-i pi / 4))
+// at tan_off<R, N>(NS, k): (m, q) pairs in `mq`, the exponent e in `te`; the inverse transform uses the
+// conjugates (q -> -q, e -> -e mod 4), and the factors W4 = -i of the radix's inner levels are
+// further powers of i.
+template <int R> struct TanEnt {
+  static constexpr int n = R == 8 ? 4 : (R == 4 ? 2 : 1);
+};
+template <int R, int N> __host__ __device__ constexpr int tan_base() {
+  return R == 2 ? 0 : (R == 4 ? (N - 1) : 3 * (N - 1));
+}
+template <int R, int N> __device__ __forceinline__ int tan_off(int ns, int k) {
+  return tan_base<R, N>() + (ns - 1 + k) * TanEnt<R>::n;
+}
+
+// a, b -> a + t b, a - t b with t = i^e m (1 + i q) (forward), its conjugate for the inverse
+__device__ __forceinline__ void bf_tan(double2& a, double2& b, double2 mq, int e, unsigned inv) {
+  const double q = flip(mq.y, inv);
+  e = (inv ? -e : e) & 3;
+  const double ux = fma(-q, b.y, b.x), uy = fma(q, b.x, b.y);
+  const bool sw = e & 1;
+  const double vx = flip(sw ? uy : ux, ((e ^ (e >> 1)) & 1) ? 0x80000000u : 0u);
+  const double vy = flip(sw ? ux : uy, (e >> 1) ? 0x80000000u : 0u);
+  const double m = mq.x;
+  const double2 a0 = a;
+  a = make_double2(fma(m, vx, a0.x), fma(m, vy, a0.y));
+  b = make_double2(fma(-m, vx, a0.x), fma(-m, vy, a0.y));
+}
+
+// X_q = sum_r v_r w^r W_R^(rq), from the stage's table entries; outputs in natural order
+template <int R> struct DftTan;
+template <> struct DftTan<2> {
+  __device__ __forceinline__ static void run(double2* v, const double2* mq, const unsigned char* te, unsigned inv) {
+    bf_tan(v[0], v[1], mq[0], te[0], inv);
+  }
+};
+template <> struct DftTan<4> {
+  __device__ __forceinline__ static void run(double2* v, const double2* mq, const unsigned char* te, unsigned inv) {
+    const double2 t2 = mq[0], t1 = mq[1];
+    const int e2 = te[0], e1 = te[1];
+    bf_tan(v[0], v[2], t2, e2, inv);
+    bf_tan(v[1], v[3], t2, e2, inv);
+    bf_tan(v[0], v[1], t1, e1, inv);            // X0, X2
+    bf_tan(v[2], v[3], t1, (e1 + 3) & 3, inv);  // X1, X3 (twiddle w W4)
+    const double2 x1 = v[2];
+    v[2] = v[1];
+    v[1] = x1;
+  }
+};
+template <> struct DftTan<8> {
+  __device__ __forceinline__ static void run(double2* v, const double2* mq, const unsigned char* te, unsigned inv) {
+    const double2 t4 = mq[0], t2 = mq[1], t1 = mq[2], t18 = mq[3];
+    const int e4 = te[0], e2 = te[1], e1 = te[2], e18 = te[3];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) bf_tan(v[j], v[j + 4], t4, e4, inv);
+    // even outputs from (v0..v3) with w, odd ones from (v4..v7) with w W8
+    bf_tan(v[0], v[2], t2, e2, inv);
+    bf_tan(v[1], v[3], t2, e2, inv);
+    bf_tan(v[4], v[6], t2, (e2 + 3) & 3, inv);
+    bf_tan(v[5], v[7], t2, (e2 + 3) & 3, inv);
+    bf_tan(v[0], v[1], t1, e1, inv);             // X0, X4
+    bf_tan(v[2], v[3], t1, (e1 + 3) & 3, inv);   // X2, X6
+    bf_tan(v[4], v[5], t18, e18, inv);           // X1, X5
+    bf_tan(v[6], v[7], t18, (e18 + 3) & 3, inv); // X3, X7
+    const double2 x4 = v[1], x1 = v[4], x2 = v[2], x6 = v[3], x5 = v[5], x3 = v[6];
+    v[1] = x1;
+    v[2] = x2;
+    v[3] = x3;
+    v[4] = x4;
+    v[5] = x5;
+    v[6] = x6;
+  }
+};
+
 // radix of a stage with REM points left to combine: at most MAXR, the number of elements a thread
 // owns when it is below 8 (every stage then gives each thread whole butterflies)
 template <int REM, int MAXR = 8> struct RadixChoice {
@@ -121,7 +212,8 @@ template <class Tile, int NT> struct MaxRadix {
 // Middle Stockham stage with span NS: shared memory to shared memory, in place
 // (all inputs are read before the barrier, all outputs written after it).
 template <class Tile, int NT, int NS, typename V>
-__device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __restrict__ tw, int tid, unsigned inv) {
+__device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __restrict__ tw, int tid, unsigned inv,
+                                               const double2* __restrict__ tmq, const unsigned char* __restrict__ te) {
   constexpr int N = Tile::N;
   constexpr int R = RadixChoice<N / NS, MaxRadix<Tile, NT>::value>::R;
   constexpr int NB = N / R;
@@ -142,9 +234,14 @@ __device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __res
     int line, b;
     split_item<Tile>(tid + m * NT, line, b);
     const int k = b & (NS - 1);
+    if constexpr (std::is_same<V, double2>::value) {
+      const int off = tan_off<R, N>(NS, k);
+      DftTan<R>::run(v[m], tmq + off, te + off, inv);
+    } else {
 #pragma unroll
-    for (int r = 1; r < R; ++r) v[m][r] = cmul_l(v[m][r], cconj_if(tw[r * k * (N / (NS * R))], inv));
-    Dft<R, V>::run(v[m], inv);
+      for (int r = 1; r < R; ++r) v[m][r] = cmul_l(v[m][r], cconj_if(tw[r * k * (N / (NS * R))], inv));
+      Dft<R, V>::run(v[m], inv);
+    }
     const int base = (b / NS) * NS * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) s[Tile::addr(line, base + r * NS)] = v[m][r];
@@ -154,11 +251,12 @@ __device__ __forceinline__ void stockham_stage(V* __restrict__ s, const V* __res
 
 template <class Tile, int NT, int NS, typename V> struct MiddleStages {
   // applies stages NS, NS*R, ... up to but excluding the last one
-  __device__ __forceinline__ static void run(V* s, const V* tw, int tid, unsigned inv) {
+  __device__ __forceinline__ static void run(V* s, const V* tw, int tid, unsigned inv, const double2* tmq,
+                                             const unsigned char* te) {
     constexpr int R = RadixChoice<Tile::N / NS, MaxRadix<Tile, NT>::value>::R;
     if constexpr (NS * R < Tile::N) {
-      stockham_stage<Tile, NT, NS, V>(s, tw, tid, inv);
-      MiddleStages<Tile, NT, NS * R, V>::run(s, tw, tid, inv);
+      stockham_stage<Tile, NT, NS, V>(s, tw, tid, inv, tmq, te);
+      MiddleStages<Tile, NT, NS * R, V>::run(s, tw, tid, inv, tmq, te);
     }
   }
 };
@@ -173,8 +271,11 @@ template <int N, int MAXR> struct LastSpan<N, N, MAXR> {
 
 // Full FFT of every line of the tile, registers in and out; inv selects the direction.
 //   r[k] holds the thread's element at position tid / LINES + k * (N / E) of line tid % LINES.
+// tmq / te: the tangent-form twiddle table of the line length (native FP64 only)
 template <class Tile, int NT, typename V>
-__device__ __forceinline__ void tile_fft_regs(V* r, V* __restrict__ s, const V* __restrict__ tw, int tid, unsigned inv) {
+__device__ __forceinline__ void tile_fft_regs(V* r, V* __restrict__ s, const V* __restrict__ tw, int tid, unsigned inv,
+                                              const double2* __restrict__ tmq = nullptr,
+                                              const unsigned char* __restrict__ te = nullptr) {
   constexpr int N = Tile::N;
   constexpr int L = Tile::LINES;
   constexpr int E = N * L / NT;
@@ -197,7 +298,7 @@ __device__ __forceinline__ void tile_fft_regs(V* r, V* __restrict__ s, const V* 
     for (int q = 0; q < R1; ++q) s[Tile::addr(line, b * R1 + q)] = v[q];
   }
   __syncthreads();
-  MiddleStages<Tile, NT, R1, V>::run(s, tw, tid, inv);
+  MiddleStages<Tile, NT, R1, V>::run(s, tw, tid, inv, tmq, te);
   // last stage: span NSL = N / RL; outputs land on the thread's own positions
   constexpr int NSL = LastSpan<N, R1, MAXR>::value;
   constexpr int RL = N / NSL;
@@ -216,9 +317,14 @@ __device__ __forceinline__ void tile_fft_regs(V* r, V* __restrict__ s, const V* 
     int line, b;
     split_item<Tile>(tid + m * NT, line, b);
     // b < NSL here, so the twiddle exponent is q * b and the outputs go to b + q * NSL
+    if constexpr (std::is_same<V, double2>::value) {
+      const int off = tan_off<RL, N>(NSL, b);
+      DftTan<RL>::run(v[m], tmq + off, te + off, inv);
+    } else {
 #pragma unroll
-    for (int q = 1; q < RL; ++q) v[m][q] = cmul_l(v[m][q], cconj_if(tw[q * b], inv));
-    Dft<RL, V>::run(v[m], inv);
+      for (int q = 1; q < RL; ++q) v[m][q] = cmul_l(v[m][q], cconj_if(tw[q * b], inv));
+      Dft<RL, V>::run(v[m], inv);
+    }
 #pragma unroll
     for (int q = 0; q < RL; ++q) r[m + q * PERL] = v[m][q];
   }

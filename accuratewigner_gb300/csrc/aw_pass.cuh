@@ -117,7 +117,10 @@ __device__ __forceinline__ void apply_factor(V* r, const AwFactor& f, int lg, in
     if (et) v = Tile::IS_ROW ? cmul_l(v, et[j]) : cmulc_l(v, et[i]);
     if (f.lin) v = cmul_l(v, ct[f.lin == 1 ? (long long)i * ncols + j : i + (long long)nrows * j]);
     if (have_c) v = cmul_l(v, c);
-    if (lo_n) {
+    if (f.sh_full) {
+      const int q = (pos + f.sh_roll) & (Tile::N - 1);
+      v = cmul_l(v, ((const V*)f.sh_full)[(long long)lg * Tile::N + q]);
+    } else if (lo_n) {
       const int q = (pos + f.sh_roll) & (Tile::N - 1);
       V w = cmul_l(sh[(long long)lg * nhi + q / lo_n], sl[(long long)lg * lo_n + (q % lo_n)]);
       v = cmul_l(v, w);
@@ -127,9 +130,10 @@ __device__ __forceinline__ void apply_factor(V* r, const AwFactor& f, int lg, in
 }
 
 template <class Tile, int NT, typename V>
-__device__ __forceinline__ void run_fft(V* r, V* s, const V* tw, int dir, int tid) {
+__device__ __forceinline__ void run_fft(V* r, V* s, const AwPassArgs& a, int dir, int tid) {
   if (dir == 0) return;
-  tile_fft_regs<Tile, NT, V>(r, s, tw, tid, dir > 0 ? 0u : 0x80000000u);
+  tile_fft_regs<Tile, NT, V>(r, s, (const V*)a.tw, tid, dir > 0 ? 0u : 0x80000000u, (const double2*)a.twt_mq,
+                             a.twt_e);
 }
 
 template <typename V, class Tile, int NT>
@@ -241,7 +245,7 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
   }
 
   if constexpr (REDUCE_ONLY) {
-    run_fft<Tile, NT>(r, s, tw, a.d1, tid);
+    run_fft<Tile, NT>(r, s, a, a.d1, tid);
     if (a.f1.active) apply_factor<V, Tile, NT>(r, a.f1, lg, pos0, a.nrows, ncols, toff, eoff, inst);
   } else {
   // The pass as a loop over FFT segments, so that the kernel holds one copy of the FFT and of
@@ -262,7 +266,7 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
     const AwFactor* post = seg == 0 ? &a.f1 : (seg == 1 ? &a.fbr : (seg == 3 ? &a.f3 : nullptr));
     const int dir = seg == 0 ? a.d1 : (seg == 1 ? a.br_d1 : (seg == 2 ? a.br_d2 : a.d2));
     if (pre && pre->active) apply_factor<V, Tile, NT>(r, *pre, lg, pos0, a.nrows, ncols, toff, eoff, inst);
-    run_fft<Tile, NT>(r, s, tw, dir, tid);
+    run_fft<Tile, NT>(r, s, a, dir, tid);
     if (post && post->active) apply_factor<V, Tile, NT>(r, *post, lg, pos0, a.nrows, ncols, toff, eoff, inst);
     if (seg == 0) {
       if (a.mid_out) store_regs<V, Tile, NT>((V*)a.mid_out + eoff, r, lg, pos0, ncols, a.mid_sign != 0);

@@ -26,6 +26,7 @@ typedef struct AwFactor {
   const void* mask;         // real, [nrows][ncols]
   const void* sh_hi;        // shear table, [lines][npos / sh_lo_n] complex
   const void* sh_lo;        // shear table, [lines][sh_lo_n] complex
+  const void* sh_full;      // or the shear factors themselves, [lines][N] complex (replaces hi x lo)
   const double* scale_ptr;  // optional device scalar: complex (re, im), one per instance
   double scale;
   int mask_pow;             // 0: no mask
@@ -42,6 +43,8 @@ typedef struct AwPassArgs {
   void* out;                // may be 0 for a reduce-only pass
   int nrows, ncols;
   const void* tw;           // twiddle table of the transform length
+  const void* twt_mq;       // native FP64: the tangent-form twiddle table of the transform length (aw_fft.cuh),
+  const unsigned char* twt_e;  // ... (m, q) pairs and exponents; required by the FP64 passes
   AwFactor f0;
   int d1;                   // 0: none, +1: forward, -1: inverse (unnormalised)
   AwFactor f1;

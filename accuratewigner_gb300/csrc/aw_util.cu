@@ -239,6 +239,16 @@ __global__ void k_sum_parts(const double2* part, int nparts, int n, double2* out
   out[k] = make_double2(sr, si);
 }
 
+// full[l][q] = hi[l][q / lo_n] * lo[l][q % lo_n] (complex128)
+__global__ void k_shear_full(const double2* hi, const double2* lo, int lo_n, int lines, int npos, double2* full) {
+  const long long n = (long long)lines * npos;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const int l = (int)(k / npos), q = (int)(k % npos);
+    const double2 a = hi[(long long)l * (npos / lo_n) + q / lo_n], b = lo[(long long)l * lo_n + q % lo_n];
+    full[k] = make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  }
+}
+
 __global__ void k_set2(double* p, double a, double b) {
   p[0] = a;
   p[1] = b;
@@ -258,6 +268,12 @@ inline int ok() { return cudaGetLastError() == cudaSuccess ? 0 : -1; }
 }  // namespace
 
 extern "C" {
+
+int aw_k_shear_full(const void* hi, const void* lo, int lo_n, int lines, int npos, void* full, void* s) {
+  k_shear_full<<<grid_for((long long)lines * npos), 256, 0, (cudaStream_t)s>>>(
+      (const double2*)hi, (const double2*)lo, lo_n, lines, npos, (double2*)full);
+  return ok();
+}
 
 int aw_k_scale(void* a, int f32, long long n, double re, double im, const double* ptr, void* s) {
   return aw_k_scale_n(a, f32, n, 1, re, im, ptr, s);
