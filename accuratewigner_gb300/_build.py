@@ -33,6 +33,10 @@ def _generated():
             text = "// generated by _build.py: %s pass kernels of line length %d\n" % (tag, n)
             text += '#include "aw_pass.cuh"\n\nAW_SIZE_LAUNCHERS(%s, %s, %d)\n' % (vt, tag, n)
             out.append((os.path.join(GEN, "aw_pass_%s_%d.cu" % (tag, n)), text))
+    for tag, vt in FORMS:
+        text = "// generated by _build.py: grouped %s pass kernels\n" % tag
+        text += '#include "aw_group.cuh"\n\nAW_GROUP_LAUNCHER(%s, %s)\n' % (vt, tag)
+        out.insert(0, (os.path.join(GEN, "aw_group_%s.cu" % tag), text))
     return out
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")

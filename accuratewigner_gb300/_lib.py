@@ -95,6 +95,7 @@ SIGNATURES = [
     ("aw_launch_count", c_i64, []),
     ("aw_profile", c_int, [c_vp, c_int]),
     ("aw_graph", c_int, [c_vp, c_int]),
+    ("aw_group_propagate", c_int, [ctypes.POINTER(c_vp), c_int, c_i64, ctypes.POINTER(c_dbl)]),
     ("aw_pass_form", c_int, [c_vp, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
     ("aw_profile_read", c_int, [c_vp, ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl), ctypes.POINTER(c_i64)]),
     ("aw_create", c_int, [ctypes.POINTER(AwConfig), ctypes.POINTER(c_vp)]),

@@ -192,3 +192,32 @@ class PropagatorBatch:
         out = _c.c_double()
         _lib.check(_lib.load().aw_purity(self._h, _c.byref(out)))
         return out.value
+
+
+def propagate_group(members, steps):
+    """Advance von Neumann propagators of different grid sizes together by `steps` real-time steps.
+
+    `members`: up to 8 RhoVNeumannCUDA1D propagators or PropagatorBatch batches of them (each batch over
+    its current view), one arithmetic form, no per-step observables, V and K independent of t.  Every
+    pass of a step is one persistent launch over the tiles of all members (aw_group_propagate); no
+    counterpart in the reference, which runs one propagator per script.  Each member's time advances.
+    """
+    members = list(members)
+    handles = (_c.c_void_p * len(members))()
+    times = (_c.c_double * len(members))()
+    for k, m in enumerate(members):
+        handles[k] = m._h
+        if isinstance(m, PropagatorBatch):
+            if m.cls is not RhoVNeumannCUDA1D:
+                raise TypeError("grouped propagation takes von Neumann propagators")
+            times[k] = float(m.t[m._view[0]])
+        else:
+            times[k] = float(m.t)
+    _lib.check(_lib.load().aw_group_propagate(handles, len(members), int(steps), times))
+    for k, m in enumerate(members):
+        if isinstance(m, PropagatorBatch):
+            first, count = m._view
+            m.t[first:first + count] += steps * m.prop.dt
+        else:
+            m.t = np.float64(times[k])
+    return members

@@ -671,9 +671,10 @@ static void df_outputs(aw_state_s* h, const AwPassArgs& a, int batch) {
   df_mark(h, df_region(a, a.br_out), n);
 }
 
-// `st`: the stream of the launch (the handle's own when null)
-static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row, cudaStream_t st = nullptr) {
-  if (!st) st = h->st;
+// The arguments a pass launch of handle h needs beyond its program: twiddle tables, batch stops, row
+// lines, the error word, and the double-float conversion of its input (shared by the grouped launch).
+static int prep_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row, cudaStream_t st) {
+  if (!row && (a.br_out || a.mid_out)) return fail(AW_E_STATE, "column passes have no branch or mid-point store");
   a.tw = tw.p;
   if (!h->df && !h->f32) {
     // the native FP64 passes take the tangent-form table of the same length
@@ -686,7 +687,6 @@ static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row,
     a.twt_mq = tt[0].p;
     a.twt_e = (const unsigned char*)tt[1].p;
   }
-  const int batch = h->vc;
   if (h->ni > 1) {
     // every pass of a batch skips the instances that are stopped or inactive, and splits its
     // columns the same way whatever the view
@@ -695,7 +695,15 @@ static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row,
   }
   if (row && !a.row_lines) a.row_lines = row_lines(h, a.nrows, a.ncols);
   a.err = h->err_dev;
-  if (h->df) TRY(df_prepare(h, a, batch, st));
+  if (h->df) TRY(df_prepare(h, a, h->vc, st));
+  return AW_OK;
+}
+
+// `st`: the stream of the launch (the handle's own when null)
+static int launch_pass(aw_state_s* h, AwPassArgs& a, const DevBuf& tw, bool row, cudaStream_t st = nullptr) {
+  if (!st) st = h->st;
+  TRY(prep_pass(h, a, tw, row, st));
+  const int batch = h->vc;
   cudaEvent_t pe = prof_mark(h, st);
   int r;
   if (h->df)
@@ -2713,6 +2721,171 @@ int vn_propagate(aw_state_s* h, long long steps, double* t) {
   TRY(vscale(h, h->rho.p, gsz(h)));
   h->hist_rows = c.ehrenfest ? steps : 0;
   *t = times[steps];
+  return AW_OK;
+}
+
+// ============================================================================ grouped propagation
+// von Neumann propagators of different grid sizes (each a single propagator or a batch) advanced
+// together (no counterpart in the reference, which runs one propagator per script): each pass of a
+// step is one persistent launch over the tiles of all of them (aw_group.cuh), the trace normalisation
+// one launch over all their instances.  The steps are rho_vneumann_cuda_1d.py:429-448 as in vn_run;
+// every member computes with 8 elements a thread (radix-8 stages) in both passes, the same bits
+// whichever other members share the launch.
+namespace {
+struct StreamSwap {  // the members' work goes to one stream for the duration of the call
+  std::vector<std::pair<aw_state_s*, cudaStream_t>> saved;
+  ~StreamSwap() {
+    for (auto& p : saved) p.first->st = p.second;
+  }
+};
+}  // namespace
+
+static int group_pass(aw_handle* hs, int count, bool row, std::vector<AwPassArgs>& args, cudaStream_t st) {
+  AwGroupArgs g;
+  memset(&g, 0, sizeof g);
+  g.count = count;
+  for (int m = 0; m < count; ++m) {
+    aw_state_s* h = hs[m];
+    TRY(prep_pass(h, args[m], row ? h->tw_r : h->tw_c, row, st));
+    const int lines = aw_group_tile_lines(row ? h->nc : h->nr);
+    g.tiles_x[m] = (row ? h->nr : h->nc) / lines;
+    g.start[m + 1] = g.start[m] + g.tiles_x[m] * h->vc;
+    g.a[m] = args[m];
+  }
+  const aw_state_s* h0 = hs[0];
+  const int r = h0->df ? aw_launch_group_df(&g, row, st) : (h0->f32 ? aw_launch_group_f32(&g, row, st)
+                                                                     : aw_launch_group_f64(&g, row, st));
+  ++g_launches;
+  if (r) return fail(AW_E_CUDA, "grouped %s pass launch failed (%d, %s)", row ? "row" : "column", r,
+                     cudaGetErrorString(cudaGetLastError()));
+  for (int m = 0; m < count; ++m)
+    if (hs[m]->df) df_outputs(hs[m], args[m], hs[m]->vc);
+  return AW_OK;
+}
+
+extern "C" int aw_group_propagate(aw_handle* hs, int32_t count, int64_t steps, double* t) {
+  if (!hs || !t) return fail(AW_E_ARG, "aw_group_propagate: null argument");
+  if (count < 1 || count > AW_GROUP_MAX) return fail(AW_E_ARG, "aw_group_propagate: 1 to %d propagators", AW_GROUP_MAX);
+  if (steps < 0) return fail(AW_E_ARG, "aw_group_propagate: negative step count");
+  for (int m = 0; m < count; ++m) {
+    aw_state_s* h = hs[m];
+    if (!h) return fail(AW_E_ARG, "aw_group_propagate: null handle %d", m);
+    for (int k = 0; k < m; ++k)
+      if (hs[k] == h) return fail(AW_E_ARG, "aw_group_propagate: handle %d appears twice", m);
+    const aw_config& c = h->cfg;
+    if (h->kind != AW_RHO_VNEUMANN)
+      return fail(AW_E_STATE, "aw_group_propagate: von Neumann propagators only (member %d)", m);
+    if (c.ehrenfest || c.v_time_dependent || c.k_time_dependent || c.absx_mode == 2 || c.absp_mode == 2)
+      return fail(AW_E_STATE, "aw_group_propagate: member %d records observables or has a time-dependent V, K or "
+                              "absorber", m);
+    if (!aw_group_tile_lines(h->nc) || h->nr != h->nc)
+      return fail(AW_E_ARG, "aw_group_propagate: grid sides 64 to 2048 (member %d: %d)", m, h->nc);
+    if (h->df != hs[0]->df || h->f32 != hs[0]->f32)
+      return fail(AW_E_ARG, "aw_group_propagate: all members in one arithmetic form");
+  }
+  for (int m = 0; m < count; ++m) CK(cudaStreamSynchronize(hs[m]->st));
+  StreamSwap swap;
+  cudaStream_t st = hs[0]->st;
+  for (int m = 1; m < count; ++m) {
+    swap.saved.push_back({hs[m], hs[m]->st});
+    hs[m]->st = st;
+  }
+  // the states go back to complex128 however the call ends (before the streams are restored)
+  std::vector<Settled> guards;
+  guards.reserve(count);
+  for (int m = 0; m < count; ++m) guards.push_back(Settled{hs[m]});
+  std::vector<std::vector<double>> times(count);
+  VnPlan p{false, 0.0, false, false, 0, 0};
+  for (int m = 0; m < count; ++m) {
+    aw_state_s* h = hs[m];
+    times[m].resize(steps + 2);
+    times[m][0] = t[m];
+    for (long long n = 1; n <= steps + 1; ++n) times[m][n] = times[m][n - 1] + h->cfg.dt;
+    TRY(ensure_hist(h, steps + 1));
+    h->hist_rows = 0;
+    if (steps == 0) continue;
+    TRY(vinv_reset(h));
+    TRY(reset_stops(h));
+    TRY(vn_tables(h, p, times[m][1], true));
+  }
+  if (steps == 0) return AW_OK;
+  std::vector<AwPassArgs> args(count);
+  auto stop_of = [&](aw_state_s* h) -> const int* { return h->ni > 1 ? (const int*)dstop(h) : nullptr; };
+  // first kick: rho (position) -> S V(t_1) -> fft1
+  for (int m = 0; m < count; ++m) {
+    aw_state_s* h = hs[m];
+    AwPassArgs a = pnone(h);
+    a.in = a.out = h->rho.p;
+    a.f2 = ftab(h, TAB_V1);
+    a.f2.sign = 1;
+    a.d2 = +1;
+    a.stop = stop_of(h);
+    args[m] = a;
+  }
+  TRY(group_pass(hs, count, true, args, st));
+  AwTraceGroup tg;
+  memset(&tg, 0, sizeof tg);
+  tg.count = count;
+  for (int m = 0; m < count; ++m) {
+    aw_state_s* h = hs[m];
+    tg.diag[m] = (const double2*)h->diag.p + (size_t)h->v0 * h->nc;
+    tg.n[m] = h->nc;
+    tg.ninst[m] = h->vc;
+    tg.dX[m] = h->cfg.dX;
+    tg.inv[m] = dinv(h, h->v0);
+    tg.stop[m] = dstop(h, h->v0);
+  }
+  for (long long n = 1; n <= steps; ++n) {
+    const bool last = n == steps;
+    for (int m = 0; m < count; ++m) {  // column pass: 1/trace, ifft0, K kick, fft0
+      aw_state_s* h = hs[m];
+      AwPassArgs a = pnone(h);
+      a.in = a.out = h->rho.p;
+      a.f0 = fnone();
+      a.f0.scale_ptr = dinv(h);
+      a.f0.active = 1;
+      a.d1 = -1;
+      a.f1 = ftab(h, TAB_K);
+      a.d2 = +1;
+      a.stop = stop_of(h);
+      args[m] = a;
+    }
+    TRY(group_pass(hs, count, false, args, st));
+    for (int m = 0; m < count; ++m) {  // row pass: ifft1, V kick, diagonal, next kick, fft1
+      aw_state_s* h = hs[m];
+      AwPassArgs a = pnone(h);
+      a.in = a.out = h->rho.p;
+      a.d1 = -1;
+      a.f1 = ftab(h, TAB_V1);
+      a.diag_out = (double2*)h->diag.p;
+      if (!last) {
+        a.f2 = ftab(h, TAB_V1);
+        a.d2 = +1;
+      } else {
+        a.f2 = fsign();
+      }
+      a.stop = stop_of(h);
+      args[m] = a;
+    }
+    TRY(group_pass(hs, count, true, args, st));
+    {
+      const int r = aw_k_trace_finalize_group(&tg, st);
+      ++g_launches;
+      if (r) return fail(AW_E_CUDA, "grouped trace launch failed (%d)", r);
+    }
+  }
+  for (int m = 0; m < count; ++m) {
+    aw_state_s* h = hs[m];
+    TRY(settle(h));
+    TRY(vscale(h, h->rho.p, gsz(h)));
+    t[m] = times[m][steps];
+  }
+  // each member's own stream continues after the group's work
+  cudaEvent_t done;
+  CK(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+  CK(cudaEventRecord(done, st));
+  for (auto& sv : swap.saved) CK(cudaStreamWaitEvent(sv.second, done, 0));
+  cudaEventDestroy(done);
   return AW_OK;
 }
 

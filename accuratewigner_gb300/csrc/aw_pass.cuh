@@ -181,29 +181,28 @@ __device__ __forceinline__ double block_sum(double x, double* red, int tid) {
 // TMA: (column tiles) the tile arrives in shared memory by tensor copies and `out` leaves it the same
 // way (aw_tma.cuh); everything between is the register-resident program of the direct form, so the
 // two forms give bit-identical results.
+// The pass program on the tile of logical block (bx, by) of a launch of gx x ... blocks; the kernel
+// below runs it for its own block, the grouped kernel (aw_group.cuh) for the work items it walks.
 template <typename V, class Tile, int NT, bool REDUCE_ONLY = false, bool TMA = false>
-__global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 1)
-                                                              : (NT <= 128 ? 5 : (NT <= 256 ? (REDUCE_ONLY ? 3 : 2) : 1))))
-    aw_pass_kernel(const __grid_constant__ AwPassArgs a) {
-  extern __shared__ __align__(128) unsigned char aw_smem[];
+__device__ __forceinline__ void aw_pass_body(const AwPassArgs& a, const int bx, const int by, const int gx,
+                                             unsigned char* aw_smem) {
   typedef typename RealOf<V>::type T;
   V* s = reinterpret_cast<V*>(aw_smem);
   constexpr int L = Tile::LINES;
   constexpr int E = Own<Tile, NT>::E;
   constexpr int STEP = Own<Tile, NT>::STEP;
   __shared__ double red[NT];
-  const int inst = blockIdx.y + a.inst0;
+  const int inst = by + a.inst0;
   if (a.stop && a.stop[inst]) return;
   const int tid = threadIdx.x;
   const int line = tid % L;
   const int pos0 = tid / L;
-  const int line0 = blockIdx.x * L;
+  const int line0 = bx * L;
   const int lg = line0 + line;
   const int ncols = a.ncols;
   const long long eoff = (long long)inst * a.batch_elems;
   const long long toff = (long long)inst * a.batch_tab;
   const V* in = (const V*)a.in + eoff;
-  const V* tw = (const V*)a.tw;
 
   // TMA geometry: 8-byte words per element, rows per box, boxes per tile; tensor row of this
   // instance's row 0 (the instances of the launch are stacked rows of one tensor)
@@ -257,7 +256,8 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
   V keep[E];
 #pragma unroll 1
   for (int seg = 0; seg < 4; ++seg) {
-    if ((seg == 1 || seg == 2) && !a.br_out) continue;
+    // column passes never branch (the host refuses it), so their kernels carry no branch code
+    if ((seg == 1 || seg == 2) && (!Tile::IS_ROW || !a.br_out)) continue;
     if (seg == 1) {
 #pragma unroll
       for (int k = 0; k < E; ++k) keep[k] = r[k];
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
     run_fft<Tile, NT>(r, s, a, dir, tid);
     if (post && post->active) apply_factor<V, Tile, NT>(r, *post, lg, pos0, a.nrows, ncols, toff, eoff, inst);
     if (seg == 0) {
-      if (a.mid_out) store_regs<V, Tile, NT>((V*)a.mid_out + eoff, r, lg, pos0, ncols, a.mid_sign != 0);
+      if (Tile::IS_ROW && a.mid_out) store_regs<V, Tile, NT>((V*)a.mid_out + eoff, r, lg, pos0, ncols, a.mid_sign != 0);
       if (Tile::IS_ROW && a.diag_out) {
 #pragma unroll
         for (int k = 0; k < E; ++k)
@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
 #pragma unroll
         for (int k = 0; k < E; ++k) acc += cabs2(r[k]);
         const double tot = block_sum<NT>(to_d(acc), red, tid);
-        if (tid == 0) a.red_abs2[(long long)inst * gridDim.x + blockIdx.x] = tot;
+        if (tid == 0) a.red_abs2[(long long)inst * gx + bx] = tot;
       }
     }
     if (seg == 2) {
@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
 #pragma unroll
     for (int k = 0; k < E; ++k) acc += cabs2(r[k]);
     const double tot = block_sum<NT>(to_d(acc), red, tid);
-    if (tid == 0) a.red_abs2[(long long)inst * gridDim.x + blockIdx.x] = tot;
+    if (tid == 0) a.red_abs2[(long long)inst * gx + bx] = tot;
   }
   }
 
@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
               reinterpret_cast<typename cpart<V>::type*>(aw_smem + sizeof(V) * Tile::SMEM_ELEMS)[pos] =
                   cpart<V>::make(xr, xi);
             else
-              a.alt_cross[((long long)inst * gridDim.x + blockIdx.x) * a.nrows + pos] = make_double2(to_d(xr), to_d(xi));
+              a.alt_cross[((long long)inst * gx + bx) * a.nrows + pos] = make_double2(to_d(xr), to_d(xi));
           }
         }
       }
@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
         for (int k = lo + tid; k < hi; k += NT) {
           P acc = cpart<V>::zero();
           for (int q = 0; q < ncl; ++q) acc = cpart<V>::add(acc, cl.map_shared_rank(mine, q)[k]);
-          a.alt_cross[((long long)inst * (gridDim.x / ncl) + blockIdx.x / ncl) * n + k] = cpart<V>::to_d2(acc);
+          a.alt_cross[((long long)inst * (gx / ncl) + bx / ncl) * n + k] = cpart<V>::to_d2(acc);
         }
         cl.sync();
       }
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
           double c = to_d(re);
 #pragma unroll
           for (int o = B / 2; o > 0; o >>= 1) c += __shfl_xor_sync(lane_mask<NT>(), c, o, B);
-          if (line == 0) a.red_cross[((long long)inst * gridDim.x + blockIdx.x) * a.nrows + pos] = c;
+          if (line == 0) a.red_cross[((long long)inst * gx + bx) * a.nrows + pos] = c;
         }
       }
       if (a.red_line) {
@@ -418,11 +418,20 @@ __global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 
       }
       if (a.red_sq) {
         const double tot = block_sum<NT>(to_d(sq), red, tid);
-        if (tid == 0) a.red_sq[(long long)inst * gridDim.x + blockIdx.x] = tot;
+        if (tid == 0) a.red_sq[(long long)inst * gx + bx] = tot;
       }
     }
   }
 }
+
+template <typename V, class Tile, int NT, bool REDUCE_ONLY = false, bool TMA = false>
+__global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 1)
+                                                              : (NT <= 128 ? 5 : (NT <= 256 ? (REDUCE_ONLY ? 3 : 2) : 1))))
+    aw_pass_kernel(const __grid_constant__ AwPassArgs a) {
+  extern __shared__ __align__(128) unsigned char aw_smem[];
+  aw_pass_body<V, Tile, NT, REDUCE_ONLY, TMA>(a, blockIdx.x, blockIdx.y, gridDim.x, aw_smem);
+}
+
 
 // ------------------------------------------------------------------ dispatch
 // Grids are sized by the SM count of the device the launch goes to (aw_sm_count, aw_common.cuh).

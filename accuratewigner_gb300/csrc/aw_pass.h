@@ -82,6 +82,17 @@ typedef struct AwPassArgs {
   alignas(64) unsigned char tmap_out[128];
 } AwPassArgs;
 
+// A grouped launch: the passes of up to AW_GROUP_MAX propagators of different line lengths (64 to
+// 2048) run by one persistent kernel, each block walking work items (a member's tile of lines) in
+// index order.  Every member computes with 256 threads of 8 elements a tile (radix-8 stages).
+#define AW_GROUP_MAX 8
+typedef struct AwGroupArgs {
+  int count;
+  int start[AW_GROUP_MAX + 1];  // first work item of each member; start[count]: the total
+  int tiles_x[AW_GROUP_MAX];    // tiles along the member's lines (its work items are tiles_x x instances)
+  AwPassArgs a[AW_GROUP_MAX];
+} AwGroupArgs;
+
 // Host-side launchers, one per precision (aw_pass_f64.cu / aw_pass_f32.cu).
 // Returns 0 on success, or a negative code when the size is unsupported.
 int aw_launch_row_pass_f64(const AwPassArgs* a, int batch, void* stream);
@@ -90,6 +101,12 @@ int aw_launch_row_pass_f32(const AwPassArgs* a, int batch, void* stream);
 int aw_launch_col_pass_f32(const AwPassArgs* a, int batch, void* stream);
 int aw_launch_row_pass_df(const AwPassArgs* a, int batch, void* stream);
 int aw_launch_col_pass_df(const AwPassArgs* a, int batch, void* stream);
+// grouped passes (row != 0: row passes): 0 on success, negative when a member's length is unsupported
+int aw_launch_group_f64(const AwGroupArgs* g, int row, void* stream);
+int aw_launch_group_f32(const AwGroupArgs* g, int row, void* stream);
+int aw_launch_group_df(const AwGroupArgs* g, int row, void* stream);
+// lines of one tile of a grouped pass for line length n (0: unsupported length)
+int aw_group_tile_lines(int n);
 // number of column blocks (rows of red_cross) the column pass uses for a given N (single instance)
 int aw_col_pass_blocks(int nrows, int ncols, int f32);
 // columns per column-pass block for `batch` instances

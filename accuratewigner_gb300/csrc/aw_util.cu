@@ -130,18 +130,11 @@ __global__ void k_psi2rho(const void* psi, int f32, int N, void* rho) {
 // purity Sum |rho|^2 dX^2 (rho_vneumann_cuda_1d.py:565-579) of the normalised
 // state follows from the row pass's |rho|^2 partials.
 // blockIdx.x = instance: diag n apart, abs2part nparts apart, inv_out 2 apart, hist hstride apart
-__global__ void k_trace_finalize(const double2* diag, int n, const double* abs2part, int nparts, double dX,
-                                 int complex_trace, double* inv_out, double* hist, long long hstride, int* stop,
-                                 int stop_on_purity) {
+// trace (and purity) of one instance: 1 / trace into inv_out, the purity and trace into hist
+__device__ __forceinline__ void trace_body(const double2* diag, int n, const double* abs2part, int nparts, double dX,
+                                           int complex_trace, double* inv_out, double* hist, int* stop,
+                                           int stop_on_purity) {
   __shared__ double rr[256], ri[256], ra[256];
-  {
-    const long long in = blockIdx.x;
-    diag += in * n;
-    if (abs2part) abs2part += in * nparts;
-    inv_out += 2 * in;
-    if (hist) hist += in * hstride;
-    if (stop) stop += in;
-  }
   if (stop && *stop) return;
   const int t = threadIdx.x;
   double sr = 0.0, si = 0.0, sa = 0.0;
@@ -168,6 +161,23 @@ __global__ void k_trace_finalize(const double2* diag, int n, const double* abs2p
     }
     if (stop && stop_on_purity && !(purity < 1.0)) *stop = 1;
   }
+}
+
+__global__ void k_trace_finalize(const double2* diag, int n, const double* abs2part, int nparts, double dX,
+                                 int complex_trace, double* inv_out, double* hist, long long hstride, int* stop,
+                                 int stop_on_purity) {
+  const long long in = blockIdx.x;
+  trace_body(diag + in * n, n, abs2part ? abs2part + in * nparts : nullptr, nparts, dX, complex_trace,
+             inv_out + 2 * in, hist ? hist + in * hstride : nullptr, stop ? stop + in : nullptr, stop_on_purity);
+}
+
+// the traces of the instances of several propagators: blockIdx.y member, blockIdx.x instance
+__global__ void k_trace_finalize_group(const AwTraceGroup g) {
+  const int m = blockIdx.y, in = blockIdx.x;
+  if (in >= g.ninst[m]) return;
+  const int n = g.n[m];
+  trace_body(g.diag[m] + (long long)in * n, n, nullptr, 0, g.dX[m], g.complex_trace, g.inv[m] + 2 * in, nullptr,
+             g.stop[m] ? g.stop[m] + in : nullptr, 0);
 }
 
 // 1 / sqrt(Sum parts * scale): renormalisation of a wave function
@@ -317,6 +327,12 @@ int aw_k_trace_finalize_n(const double2* diag, int n, const double* abs2part, in
                           void* s) {
   k_trace_finalize<<<ninst, 256, 0, (cudaStream_t)s>>>(diag, n, abs2part, nparts, dX, complex_trace, inv_out, hist,
                                                        hstride, stop, stop_on_purity);
+  return ok();
+}
+int aw_k_trace_finalize_group(const AwTraceGroup* g, void* s) {
+  int most = 1;
+  for (int m = 0; m < g->count; ++m) most = g->ninst[m] > most ? g->ninst[m] : most;
+  k_trace_finalize_group<<<dim3(most, g->count), 256, 0, (cudaStream_t)s>>>(*g);
   return ok();
 }
 int aw_k_norm_finalize(const double* parts, int nparts, double scale, double* inv_out, double* hist, void* s) {

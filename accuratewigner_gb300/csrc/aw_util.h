@@ -24,6 +24,16 @@ int aw_k_trace_finalize_n(const double2* diag, int n, const double* abs2part, in
                           double* inv_out, double* hist, long long hstride, int* stop, int stop_on_purity, int ninst,
                           void* s);
 int aw_k_set2(double* p, double a, double b, void* s);
+// 1 / trace of every instance of up to 8 propagators (the grouped von Neumann step), member by member
+typedef struct AwTraceGroup {
+  int count, complex_trace;
+  const double2* diag[8];
+  int n[8], ninst[8];
+  double dX[8];
+  double* inv[8];
+  int* stop[8];
+} AwTraceGroup;
+int aw_k_trace_finalize_group(const AwTraceGroup* g, void* s);
 int aw_k_sum_parts(const double2* part, int nparts, int n, double2* out, void* s);
 int aw_k_norm_finalize(const double* parts, int nparts, double scale, double* inv_out, double* hist, void* s);
 int aw_k_abs2(const void* a, int f32, long long n, double* out, void* s);

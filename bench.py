@@ -26,6 +26,8 @@ Other workloads (one JSON line each, not the headline):
                             FP64 side by side: errors of W and of <x>, <p>, dipole acceleration per step
   --workload frames         the headline workload writing a frame (W, t, diagonal of rho) every 100
                             steps through the asynchronous run record, against no frames
+  --workload group          five von Neumann propagators of sides 128 to 2048 stepped as one group
+                            (one persistent launch per pass), against one after another
 """
 import argparse
 import ctypes
@@ -629,8 +631,21 @@ def run_served(args):
            "potential": "c2 x^2 + c3 x^3 + c4 x^4, c2 ~ U(0.1, 1), c3 ~ U(-0.02, 0.02), c4 ~ U(0, 0.05)",
            "amplitude": "X_amplitude = P_amplitude = sqrt(pi N / 2)", "chunk_steps": 200,
            "precision": args.precision},
-          {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
-           "mean_latency_s": float(lat.mean()), "p50_latency_by_kind_s": by_kind, "clocks": clk.summary()})
+          dict({"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+                "mean_latency_s": float(lat.mean()), "p50_latency_by_kind_s": by_kind, "clocks": clk.summary()},
+               **auto_summary(reqs)))
+
+
+def auto_summary(reqs):
+    """Requests of an auto engine: how many ran in each form and the measured complex64 error estimates."""
+    est = [r.est_error for r in reqs if r.est_error is not None]
+    if not est:
+        return {}
+    return {"auto": {"complex64": sum(1 for r in reqs if r.precision == "c64"),
+                     "fell_back_to_complex128": sum(1 for r in reqs if r.fell_back),
+                     "complex128_from_the_start": sum(1 for r in reqs if r.est_error is None),
+                     "est_error_p50": float(np.percentile(est, 50)), "est_error_max": float(np.max(est)),
+                     "tolerance": float(reqs[0].tol)}}
 
 
 def run_served_sweep(args):
@@ -718,6 +733,47 @@ def run_frames(args):
            "note": "frames go to a temporary directory; once the host file system's write rate is below "
                    "the frame rate the drain, not the capture, sets the time",
            "clocks": clk.summary()})
+
+
+def run_group(args):
+    """Von Neumann propagators of sides 128, 256, 512, 1024 and 2048 (one each, their own potentials),
+    200 steps: grouped (one persistent launch per pass of a step for all five) against the same
+    propagators stepped one after another through propagate()."""
+    import torch
+
+    from accuratewigner_gb300 import RhoVNeumannCUDA1D
+    from accuratewigner_gb300.batch import propagate_group
+
+    sides = [128, 256, 512, 1024, 2048]
+    steps = 200
+    init = ("exp(-0.5 * pow(X - x0, 2) - 0.5 * pow(X_prime - x0, 2)) * "
+            "exp(cuda_complex(0., p0) * (X - X_prime))")
+
+    def make():
+        out = []
+        for k, n in enumerate(sides):
+            a = float(np.sqrt(np.pi * n / 2.0))
+            g = RhoVNeumannCUDA1D(t=0.0, dt=0.01, X_gridDIM=n, X_amplitude=a, x0=0.3 * k, p0=-0.2 * k,
+                                  c2=0.2 + 0.1 * k, K="0.5 * P * P", V="c2 * X * X + 0.01 * X * X * X * X",
+                                  precision=args.precision)
+            g.set_rho(init)
+            out.append(g)
+        return out
+
+    work = float(sum(n * n for n in sides)) * steps
+    props = make()
+    propagate_group(props, 3)  # warm-up
+    with ClockSampler(0) as clk:
+        t_group, _ = _timed(lambda: [propagate_group(props, CHUNK) for _ in range(steps // CHUNK)])
+    for g in props:
+        g.propagate(3)
+    t_seq, _ = _timed(lambda: [[g.propagate(CHUNK) for g in props] for _ in range(steps // CHUNK)])
+    for g in props:
+        g.close()
+    _line("group", "grid-pt*steps/s (five von Neumann propagators of sides 128-2048 stepped as one group)",
+          work / t_group, "grid-pt*steps/s", t_group, args,
+          {"sides": sides, "steps": steps, "steps_per_call": CHUNK, "precision": args.precision},
+          {"one_after_another": work / t_seq, "speedup": t_seq / t_group, "clocks": clk.summary()})
 
 
 def large_vn_config(n=4096):
@@ -822,7 +878,7 @@ def main():
                          "cudaProfilerStart/Stop range (for ncu --profile-from-start off) and exit")
     ap.add_argument("--workload", default="strong-field",
                     choices=["strong-field", "plain", "batched-gibbs", "served", "served-sweep", "large-vn",
-                             "precision", "frames"])
+                             "precision", "frames", "group"])
     ap.add_argument("--requests", type=int, default=60, help="served: number of requests (per rate for the sweep)")
     ap.add_argument("--rate", type=float, default=4.0, help="served: Poisson arrival rate per second")
     ap.add_argument("--rates", default="1,1.5,2,3,4", help="served-sweep: comma-separated arrival rates per second")
@@ -831,7 +887,7 @@ def main():
         args.warmup = 3
     other = {"plain": run_plain, "batched-gibbs": run_batched_gibbs, "served": run_served,
              "served-sweep": run_served_sweep, "large-vn": run_large_vn, "precision": run_precision,
-             "frames": run_frames}
+             "frames": run_frames, "group": run_group}
     if args.precision == "auto" and args.workload not in ("served", "served-sweep"):
         ap.error("--precision auto chooses per request: only the served workload has requests")
     if args.profile_steps:

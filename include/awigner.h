@@ -169,6 +169,21 @@ int aw_pass_form(aw_handle h, const int32_t* set, int32_t* get);
  * on. */
 int aw_graph(aw_handle h, int32_t enable);
 
+/* Grouped propagation (no counterpart in the reference, which runs one
+ * propagator per script): `steps` real-time steps of `count` (1 to 8) von
+ * Neumann handles of different square grid sizes (sides 64 to 2048, powers of
+ * two; each handle a single propagator or a batch, over its current view), as
+ * aw_propagate does for each (rho_vneumann_cuda_1d.py:429-448), with every pass
+ * of a step ONE persistent launch over the tiles of all of them and the trace
+ * normalisation one launch over all their instances.  Members must share one
+ * arithmetic form and record no per-step observables; V, K and absorbers must
+ * not depend on t.  t[k] is member k's time, advanced on return.  Every member
+ * computes with 8 elements a thread (radix-8 FFT stages) in both passes and
+ * gives the same bits alone (a group of one) as in any group; against its own
+ * aw_propagate with those shapes (aw_pass_form) it agrees to rounding.  The work
+ * runs on the first member's stream; each member's stream waits for it. */
+int aw_group_propagate(aw_handle* handles, int32_t count, int64_t steps, double* t);
+
 #define AW_PROF_CLASSES 5
 int aw_profile(aw_handle h, int32_t enable);
 int aw_profile_read(aw_handle h, double* ms, double* bytes, int64_t* launches);
