@@ -198,9 +198,11 @@ def propagate_group(members, steps):
     """Advance von Neumann propagators of different grid sizes together by `steps` real-time steps.
 
     `members`: up to 8 RhoVNeumannCUDA1D propagators or PropagatorBatch batches of them (each batch over
-    its current view), one arithmetic form, no per-step observables, V and K independent of t.  Every
-    pass of a step is one persistent launch over the tiles of all members (aw_group_propagate); no
-    counterpart in the reference, which runs one propagator per script.  Each member's time advances.
+    its current view), one arithmetic form, no per-step observables, V and K independent of t.  Members
+    of side up to 128 (complex64: 256) step together, every pass of a step one persistent launch over
+    all their tiles; larger members run their own step loop on their own streams meanwhile
+    (aw_group_propagate).  No counterpart in the reference, which runs one propagator per script.  Each
+    member's time advances.
     """
     members = list(members)
     handles = (_c.c_void_p * len(members))()

@@ -1787,10 +1787,15 @@ static int launch_finalize_args(aw_state_s* h, const FinalArgs& f, double t, dou
   const double* tc = (const double*)((const char*)h->terms.p + 64 * 3 * sizeof(int));
   int nterms = (int)h->tslot.size(), nslots = h->cfg.n_slots;
   int cstride = f.cstride, proll = f.proll, pown = f.pnorm_own, sq = f.sqrt_norm;
+  double* tv = dtv(h, h->v0);
+  unsigned int* counter = dcounter(h, h->v0);
+  // chunks per term: at least 16 columns or rows each, as the rotated frame's reduction
+  int nchunk = std::max(1, std::min(64, std::max(ncol, nrow) / 16));
+  while (nchunk > 1 && (nterms + 3) * nchunk > 1024) nchunk >>= 1;
   void* args[] = {&colsum, &rowpart, &nparts, &sqpart, &rowsum, &hist_row, &inv, &stop, &stop_on_purity, &t,
                   &ncol, &nrow, &dX, &dP, &dXdP, &ts, &tk, &ti, &tc, &nterms, &nslots, &cstride, &proll, &pown, &sq,
-                  &prm};
-  return hjit(h, h->k_final, dim3(1), dim3(256), args);
+                  &prm, &tv, &counter, &nchunk};
+  return hjit(h, h->k_final, dim3((nterms + 3) * nchunk), dim3(128), args);
 }
 
 // rotated frame: marginals of W from the reducing column pass
@@ -2726,11 +2731,17 @@ int vn_propagate(aw_state_s* h, long long steps, double* t) {
 
 // ============================================================================ grouped propagation
 // von Neumann propagators of different grid sizes (each a single propagator or a batch) advanced
-// together (no counterpart in the reference, which runs one propagator per script): each pass of a
-// step is one persistent launch over the tiles of all of them (aw_group.cuh), the trace normalisation
-// one launch over all their instances.  The steps are rho_vneumann_cuda_1d.py:429-448 as in vn_run;
-// every member computes with 8 elements a thread (radix-8 stages) in both passes, the same bits
-// whichever other members share the launch.
+// together (no counterpart in the reference, which runs one propagator per script).  Short members
+// (group_own below): each pass of a step is one persistent launch over the tiles of all of them
+// (aw_group.cuh), the trace normalisation one launch over all their instances; the steps are
+// rho_vneumann_cuda_1d.py:429-448 as in vn_run, every member computing with 8 elements a thread
+// (radix-8 stages) in both passes, the same bits whichever other members share the launch.  Longer
+// members fill the GPU with their own launches: they run their own step loop (vn_propagate, the bits
+// of aw_propagate) on their own streams, concurrently with the grouped launches.
+//   Measured against the same propagators each through its own propagate() on its own stream (which
+// the device overlaps), 8 members of one side: complex64 1.9x (64), 1.8x (128), 1.3x (256); double-float
+// 1.5x, 1.4x, 0.94x; native FP64 1.2x, 1.3x, 0.78x; members of 512 and more ran at 0.6-0.97x grouped.
+static bool group_own(const aw_state_s* h) { return h->nc > (h->f32 ? 256 : 128); }
 namespace {
 struct StreamSwap {  // the members' work goes to one stream for the duration of the call
   std::vector<std::pair<aw_state_s*, cudaStream_t>> saved;
@@ -2746,6 +2757,11 @@ static int group_pass(aw_handle* hs, int count, bool row, std::vector<AwPassArgs
   g.count = count;
   for (int m = 0; m < count; ++m) {
     aw_state_s* h = hs[m];
+    const AwPassArgs& q = args[m];
+    // the grouped kernel is compiled without these outputs (aw_pass_body's LEAN form)
+    if (q.br_out || q.mid_out || q.red_abs2 || q.red_line || q.red_cross || q.red_sq || q.col_alt || q.alt_cross ||
+        q.tma || q.cluster > 1)
+      return fail(AW_E_STATE, "grouped passes store no branch, mid-point or reduction outputs");
     TRY(prep_pass(h, args[m], row ? h->tw_r : h->tw_c, row, st));
     const int lines = aw_group_tile_lines(row ? h->nc : h->nr);
     g.tiles_x[m] = (row ? h->nr : h->nc) / lines;
@@ -2763,6 +2779,8 @@ static int group_pass(aw_handle* hs, int count, bool row, std::vector<AwPassArgs
   return AW_OK;
 }
 
+static int group_run(aw_handle* hs, int count, int64_t steps, double** tp);
+
 extern "C" int aw_group_propagate(aw_handle* hs, int32_t count, int64_t steps, double* t) {
   if (!hs || !t) return fail(AW_E_ARG, "aw_group_propagate: null argument");
   if (count < 1 || count > AW_GROUP_MAX) return fail(AW_E_ARG, "aw_group_propagate: 1 to %d propagators", AW_GROUP_MAX);
@@ -2778,11 +2796,28 @@ extern "C" int aw_group_propagate(aw_handle* hs, int32_t count, int64_t steps, d
     if (c.ehrenfest || c.v_time_dependent || c.k_time_dependent || c.absx_mode == 2 || c.absp_mode == 2)
       return fail(AW_E_STATE, "aw_group_propagate: member %d records observables or has a time-dependent V, K or "
                               "absorber", m);
-    if (!aw_group_tile_lines(h->nc) || h->nr != h->nc)
+    if (h->nc < 64 || h->nc > 2048 || (h->nc & (h->nc - 1)) || h->nr != h->nc)
       return fail(AW_E_ARG, "aw_group_propagate: grid sides 64 to 2048 (member %d: %d)", m, h->nc);
     if (h->df != hs[0]->df || h->f32 != hs[0]->f32)
       return fail(AW_E_ARG, "aw_group_propagate: all members in one arithmetic form");
   }
+  // the large members: their own step loops, enqueued first on their own streams
+  std::vector<aw_state_s*> grouped;
+  std::vector<double*> gt;
+  for (int m = 0; m < count; ++m) {
+    if (group_own(hs[m])) {
+      Settled guard{hs[m]};
+      TRY(vn_propagate(hs[m], steps, &t[m]));
+    } else {
+      grouped.push_back(hs[m]);
+      gt.push_back(&t[m]);
+    }
+  }
+  return grouped.empty() ? AW_OK : group_run(grouped.data(), (int)grouped.size(), steps, gt.data());
+}
+
+// the grouped launches of the short members (validated by aw_group_propagate)
+static int group_run(aw_handle* hs, int count, int64_t steps, double** tp) {
   for (int m = 0; m < count; ++m) CK(cudaStreamSynchronize(hs[m]->st));
   StreamSwap swap;
   cudaStream_t st = hs[0]->st;
@@ -2799,7 +2834,7 @@ extern "C" int aw_group_propagate(aw_handle* hs, int32_t count, int64_t steps, d
   for (int m = 0; m < count; ++m) {
     aw_state_s* h = hs[m];
     times[m].resize(steps + 2);
-    times[m][0] = t[m];
+    times[m][0] = *tp[m];
     for (long long n = 1; n <= steps + 1; ++n) times[m][n] = times[m][n - 1] + h->cfg.dt;
     TRY(ensure_hist(h, steps + 1));
     h->hist_rows = 0;
@@ -2878,7 +2913,7 @@ extern "C" int aw_group_propagate(aw_handle* hs, int32_t count, int64_t steps, d
     aw_state_s* h = hs[m];
     TRY(settle(h));
     TRY(vscale(h, h->rho.p, gsz(h)));
-    t[m] = times[m][steps];
+    *tp[m] = times[m][steps];
   }
   // each member's own stream continues after the group's work
   cudaEvent_t done;

@@ -67,9 +67,12 @@ __device__ __forceinline__ dfr shfl_xor(unsigned m, dfr v, int o, int w) {
   return dfr{__shfl_xor_sync(m, v.h, o, w), __shfl_xor_sync(m, v.l, o, w)};
 }
 
-// accumulator of per-thread partial sums: FP64 for the native types, double-float for dfc
+// accumulator of per-thread partial sums (at most 16 terms; FP64 across threads): FP64 for double2,
+// double-float for dfc, FP32 for float2 -- an FP64 operation per element runs at GB300's FP64 rate
+// (2 lanes a clock a SM) and made the complex64 4096^2 reduction pass FP64-bound (241 us)
 template <typename V> struct acc_of { typedef double type; };
 template <> struct acc_of<dfc> { typedef dfr type; };
+template <> struct acc_of<float2> { typedef float type; };
 template <typename A> __device__ __forceinline__ A to_acc(double v) { return from_double<A>(v); }
 template <typename A> __device__ __forceinline__ A to_acc(float v) { return (A)(double)v; }
 template <> __device__ __forceinline__ dfr to_acc<dfr>(float v) { return df_from_float(v); }

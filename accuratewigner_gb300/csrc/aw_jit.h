@@ -244,7 +244,11 @@ extern "C" __global__ void aw_values(double* aw_out, int aw_fn, int aw_n, double
 // aw_pnorm_own), as wigner_moyal_cuda_1d.py:608-622 normalises W.  The kernel
 // also writes the purity 2 pi Sum W^2 dXdP / norm^2 (rotated frame), the norm,
 // and the factor the next pass applies: 1 / norm (or 1 / sqrt(norm) when
-// aw_sqrt_norm, for a wave function).
+// aw_sqrt_norm, for a wave function), and the P-marginal aw_rowsum.
+// Blocks: (term, X norm, P norm, sum of squares) x chunk of columns or rows, so that the FP64
+// expression work spreads over the SMs (one block took 138 us for the 4096-point von Neumann
+// observables); each block's partial goes to aw_tv, and the last block to finish adds them in a fixed
+// order.
 extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw_rowpart, int aw_nparts,
                                        const double* aw_sqpart, double* aw_rowsum, double* aw_hist,
                                        double* aw_inv_norm, int* aw_stop, int aw_stop_on_purity, double t,
@@ -252,53 +256,77 @@ extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw
                                        const int* aw_tslot, const int* aw_tkind, const int* aw_tidx,
                                        const double* aw_tcoef, int aw_nterms, int aw_nslots,
                                        int aw_cstride, int aw_proll, int aw_pnorm_own, int aw_sqrt_norm,
-                                       const double* aw_prm) {
+                                       const double* aw_prm, double* aw_tv, unsigned int* aw_counter, int aw_nchunk) {
   __shared__ double aw_red[256];
-  __shared__ double aw_tv[64];
+  __shared__ double aw_fsum[67];
+  __shared__ int aw_is_last;
   if (aw_stop && *aw_stop) return;
+  const int aw_q = blockIdx.x / aw_nchunk;  // < nterms: a term; nterms: X norm; +1: P norm; +2: squares
+  const int aw_c = blockIdx.x - aw_q * aw_nchunk;
   const int aw_t = threadIdx.x;
   const int aw_nt = blockDim.x;
-  for (int aw_i = aw_t; aw_i < aw_nrow; aw_i += aw_nt) {
-    double aw_s = 0.0;
-    for (int aw_p = 0; aw_p < aw_nparts; ++aw_p) aw_s += aw_rowpart[(long long)aw_p * aw_nrow + aw_i];
-    aw_rowsum[aw_i] = aw_s;
-  }
-  __syncthreads();
+  const bool aw_on_rows = (aw_q < aw_nterms && aw_tkind[aw_q] != 0) || aw_q == aw_nterms + 1;
+  const int aw_n = aw_on_rows ? aw_nrow : aw_ncol;
+  const int aw_len = (aw_n + aw_nchunk - 1) / aw_nchunk;
+  const int aw_lo = aw_c * aw_len;
+  const int aw_hi = aw_lo + aw_len < aw_n ? aw_lo + aw_len : aw_n;
   double aw_s = 0.0;
-  for (int aw_j = aw_t; aw_j < aw_ncol; aw_j += aw_nt) aw_s += aw_colsum[(long long)aw_j * aw_cstride];
-  const double aw_norm_raw = aw_block_sum(aw_s, aw_red);
-  aw_s = 0.0;
-  for (int aw_i = aw_t; aw_i < aw_nrow; aw_i += aw_nt) aw_s += aw_rowsum[aw_i];
-  const double aw_pnorm_raw = aw_block_sum(aw_s, aw_red);
-  aw_s = 0.0;
-  if (aw_sqpart)
-    for (int aw_p = aw_t; aw_p < aw_nparts; aw_p += aw_nt) aw_s += aw_sqpart[aw_p];
-  const double aw_sq = aw_block_sum(aw_s, aw_red);
-  for (int aw_k = 0; aw_k < aw_nterms && aw_k < 64; ++aw_k) {
-    aw_s = 0.0;
-    const int aw_idx = aw_tidx[aw_k];
-    if (aw_tkind[aw_k] == 0) {
-      for (int aw_j = aw_t; aw_j < aw_ncol; aw_j += aw_nt) {
+  if (aw_q < aw_nterms) {
+    const int aw_idx = aw_tidx[aw_q];
+    if (!aw_on_rows) {
+      for (int aw_j = aw_lo + aw_t; aw_j < aw_hi; aw_j += aw_nt) {
         const double X = aw_dX * ((aw_size_t)aw_j - 0.5 * aw_ncol);
         aw_s += aw_colsum[(long long)aw_j * aw_cstride] * aw_obs_x(aw_idx, X, t, aw_prm);
       }
     } else {
-      for (int aw_i = aw_t; aw_i < aw_nrow; aw_i += aw_nt) {
+      for (int aw_i = aw_lo + aw_t; aw_i < aw_hi; aw_i += aw_nt) {
+        double aw_r = 0.0;
+        for (int aw_p = 0; aw_p < aw_nparts; ++aw_p) aw_r += aw_rowpart[(long long)aw_p * aw_nrow + aw_i];
         const double P = aw_dP * ((aw_size_t)((aw_i + aw_proll) % aw_nrow) - 0.5 * aw_nrow);
-        aw_s += aw_rowsum[aw_i] * aw_obs_p(aw_idx, P, t, aw_prm);
+        aw_s += aw_r * aw_obs_p(aw_idx, P, t, aw_prm);
       }
     }
-    const double aw_v = aw_block_sum(aw_s, aw_red);
-    if (aw_t == 0) aw_tv[aw_k] = aw_v;
-  }
-  if (aw_t == 0) {
-    const double aw_norm = aw_norm_raw * aw_dXdP;
-    for (int aw_q = 0; aw_q < aw_nslots; ++aw_q) aw_hist[aw_q] = 0.0;
-    for (int aw_k = 0; aw_k < aw_nterms && aw_k < 64; ++aw_k) {
-      const bool aw_own = aw_pnorm_own && aw_tkind[aw_k] == 1;
-      aw_hist[aw_tslot[aw_k]] += aw_tcoef[aw_k] * (aw_own ? aw_tv[aw_k] / aw_pnorm_raw : aw_tv[aw_k] * aw_dXdP / aw_norm);
+  } else if (aw_q == aw_nterms) {
+    for (int aw_j = aw_lo + aw_t; aw_j < aw_hi; aw_j += aw_nt) aw_s += aw_colsum[(long long)aw_j * aw_cstride];
+  } else if (aw_q == aw_nterms + 1) {
+    for (int aw_i = aw_lo + aw_t; aw_i < aw_hi; aw_i += aw_nt) {
+      double aw_r = 0.0;
+      for (int aw_p = 0; aw_p < aw_nparts; ++aw_p) aw_r += aw_rowpart[(long long)aw_p * aw_nrow + aw_i];
+      aw_rowsum[aw_i] = aw_r;
+      aw_s += aw_r;
     }
-    const double aw_purity = 2.0 * M_PI * aw_sq * aw_dXdP / (aw_norm * aw_norm);
+  } else if (aw_sqpart) {
+    for (int aw_p = aw_c * aw_nt + aw_t; aw_p < aw_nparts; aw_p += aw_nt * aw_nchunk) aw_s += aw_sqpart[aw_p];
+  }
+  const double aw_v = aw_block_sum(aw_s, aw_red);
+  if (aw_t == 0) {
+    aw_tv[blockIdx.x] = aw_v;
+    __threadfence();
+    const unsigned int aw_prev = atomicAdd(aw_counter, 1u);
+    aw_is_last = aw_prev == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!aw_is_last) return;
+  __threadfence();
+  // one warp per term (or norm, or squares): lanes sum over the chunks, then a shuffle tree
+  const volatile double* aw_vt = aw_tv;
+  const int aw_lane = aw_t & 31;
+  for (int aw_k = aw_t >> 5; aw_k < aw_nterms + 3; aw_k += aw_nt >> 5) {
+    double aw_acc = 0.0;
+    for (int aw_cc = aw_lane; aw_cc < aw_nchunk; aw_cc += 32) aw_acc += aw_vt[aw_k * aw_nchunk + aw_cc];
+    for (int aw_o = 16; aw_o > 0; aw_o >>= 1) aw_acc += __shfl_down_sync(0xffffffffu, aw_acc, aw_o);
+    if (aw_lane == 0) aw_fsum[aw_k] = aw_acc;
+  }
+  __syncthreads();
+  if (aw_t == 0) {
+    const double aw_norm = aw_fsum[aw_nterms] * aw_dXdP;
+    const double aw_pnorm_raw = aw_fsum[aw_nterms + 1];
+    for (int aw_q2 = 0; aw_q2 < aw_nslots; ++aw_q2) aw_hist[aw_q2] = 0.0;
+    for (int aw_k = 0; aw_k < aw_nterms; ++aw_k) {
+      const bool aw_own = aw_pnorm_own && aw_tkind[aw_k] == 1;
+      aw_hist[aw_tslot[aw_k]] += aw_tcoef[aw_k] * (aw_own ? aw_fsum[aw_k] / aw_pnorm_raw : aw_fsum[aw_k] * aw_dXdP / aw_norm);
+    }
+    const double aw_purity = 2.0 * M_PI * aw_fsum[aw_nterms + 2] * aw_dXdP / (aw_norm * aw_norm);
     aw_hist[aw_nslots] = aw_purity;
     aw_hist[aw_nslots + 1] = aw_norm;
     if (aw_inv_norm) {
@@ -306,6 +334,7 @@ extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw
       aw_inv_norm[1] = 0.0;
     }
     if (aw_stop && aw_stop_on_purity && !(aw_purity < 1.0)) *aw_stop = 1;
+    *aw_counter = 0u;
   }
 }
 )AWSRC";

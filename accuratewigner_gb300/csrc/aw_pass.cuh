@@ -174,16 +174,22 @@ __device__ __forceinline__ double block_sum(double x, double* red, int tid) {
 // Register budget: 5 blocks of 128 threads (96 registers a thread) or 2 blocks of 256 per SM, and 4
 // blocks of 256 (64 registers) for 4 elements a thread.  The double-float passes are latency-bound
 // and the occupancy gained beats the few spills (measured on the 1024-point passes: 4 blocks of 128
-// threads 0.180 ms a step, 5 blocks 0.174, 6 blocks 0.183).
+// threads 0.180 ms a step, 5 blocks 0.174, 6 blocks 0.183).  Complex64 passes over lines of 512 points
+// and more with at most 8 elements a thread get 64 registers (1024 threads a SM; no spills in the main
+// passes): the 1024^2 Wigner-Moyal step 0.088 -> 0.074 ms, 4096^2 von Neumann 1.43 -> 1.26 ms, the
+// 64 x 512^2 Gibbs batch +16 %; at 256 points it lost 5 %.
 // REDUCE_ONLY: the reduction-only column pass (load, FFT d1, f1, column reductions, nothing stored),
 // compiled without the segment loop so that its code is a fraction of the full pass's; it needs
 // fewer registers and runs 3 blocks of 256 threads a SM (0.1555 -> 0.1537 ms a step).
 // TMA: (column tiles) the tile arrives in shared memory by tensor copies and `out` leaves it the same
 // way (aw_tma.cuh); everything between is the register-resident program of the direct form, so the
 // two forms give bit-identical results.
+// LEAN: (grouped launches) compiled without the branch segments, the mid-point and |v|^2 outputs and the
+// column reductions, which a grouped pass never asks for (the host refuses them): six tile lengths of
+// the full program in one kernel spill 700-800 bytes a thread, the lean ones 0-90.
 // The pass program on the tile of logical block (bx, by) of a launch of gx x ... blocks; the kernel
 // below runs it for its own block, the grouped kernel (aw_group.cuh) for the work items it walks.
-template <typename V, class Tile, int NT, bool REDUCE_ONLY = false, bool TMA = false>
+template <typename V, class Tile, int NT, bool REDUCE_ONLY = false, bool TMA = false, bool LEAN = false>
 __device__ __forceinline__ void aw_pass_body(const AwPassArgs& a, const int bx, const int by, const int gx,
                                              unsigned char* aw_smem) {
   typedef typename RealOf<V>::type T;
@@ -257,7 +263,7 @@ __device__ __forceinline__ void aw_pass_body(const AwPassArgs& a, const int bx, 
 #pragma unroll 1
   for (int seg = 0; seg < 4; ++seg) {
     // column passes never branch (the host refuses it), so their kernels carry no branch code
-    if ((seg == 1 || seg == 2) && (!Tile::IS_ROW || !a.br_out)) continue;
+    if ((seg == 1 || seg == 2) && (LEAN || !Tile::IS_ROW || !a.br_out)) continue;
     if (seg == 1) {
 #pragma unroll
       for (int k = 0; k < E; ++k) keep[k] = r[k];
@@ -269,14 +275,14 @@ __device__ __forceinline__ void aw_pass_body(const AwPassArgs& a, const int bx, 
     run_fft<Tile, NT>(r, s, a, dir, tid);
     if (post && post->active) apply_factor<V, Tile, NT>(r, *post, lg, pos0, a.nrows, ncols, toff, eoff, inst);
     if (seg == 0) {
-      if (Tile::IS_ROW && a.mid_out) store_regs<V, Tile, NT>((V*)a.mid_out + eoff, r, lg, pos0, ncols, a.mid_sign != 0);
+      if (!LEAN && Tile::IS_ROW && a.mid_out) store_regs<V, Tile, NT>((V*)a.mid_out + eoff, r, lg, pos0, ncols, a.mid_sign != 0);
       if (Tile::IS_ROW && a.diag_out) {
 #pragma unroll
         for (int k = 0; k < E; ++k)
           if (pos0 + k * STEP == lg)
             a.diag_out[(long long)inst * a.nrows + lg] = make_double2(to_d(cre(r[k])), to_d(cim(r[k])));
       }
-      if (a.red_abs2 && !a.abs2_end) {
+      if (!LEAN && a.red_abs2 && !a.abs2_end) {
         T acc = from_double<T>(0.0);
 #pragma unroll
         for (int k = 0; k < E; ++k) acc += cabs2(r[k]);
@@ -307,7 +313,7 @@ __device__ __forceinline__ void aw_pass_body(const AwPassArgs& a, const int bx, 
       store_regs<V, Tile, NT>((V*)a.out + eoff, r, lg, pos0, ncols, false);
     }
   }
-  if (a.red_abs2 && a.abs2_end) {
+  if (!LEAN && a.red_abs2 && a.abs2_end) {
     T acc = from_double<T>(0.0);
 #pragma unroll
     for (int k = 0; k < E; ++k) acc += cabs2(r[k]);
@@ -316,7 +322,7 @@ __device__ __forceinline__ void aw_pass_body(const AwPassArgs& a, const int bx, 
   }
   }
 
-  if constexpr (!Tile::IS_ROW) {
+  if constexpr (!Tile::IS_ROW && !LEAN) {
     constexpr int B = L;
     // per-thread partials over the thread's E elements of its column (working precision), then
     // FP64 across threads in a fixed order
@@ -395,10 +401,13 @@ __device__ __forceinline__ void aw_pass_body(const AwPassArgs& a, const int bx, 
         lsum += re;
         sq += re * re - im * im;
         if (a.red_cross) {
-          double c = to_d(re);
+          // across the block's B columns: FP32 for complex64 (B <= 16 terms), FP64 otherwise
+          typedef typename std::conditional<std::is_same<A, float>::value, float, double>::type C;
+          C c;
+          if constexpr (std::is_same<C, float>::value) c = re; else c = to_d(re);
 #pragma unroll
-          for (int o = B / 2; o > 0; o >>= 1) c += __shfl_xor_sync(lane_mask<NT>(), c, o, B);
-          if (line == 0) a.red_cross[((long long)inst * gx + bx) * a.nrows + pos] = c;
+          for (int o = B / 2; o > 0; o >>= 1) c += shfl_xor(lane_mask<NT>(), c, o, B);
+          if (line == 0) a.red_cross[((long long)inst * gx + bx) * a.nrows + pos] = (double)c;
         }
       }
       if (a.red_line) {
@@ -425,7 +434,9 @@ __device__ __forceinline__ void aw_pass_body(const AwPassArgs& a, const int bx, 
 }
 
 template <typename V, class Tile, int NT, bool REDUCE_ONLY = false, bool TMA = false>
-__global__ void __launch_bounds__(NT, (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 1)
+__global__ void __launch_bounds__(NT, (std::is_same<V, float2>::value && Tile::N >= 512 && NT >= 64 &&
+                                       (Own<Tile, NT>::E <= 8 || TMA || REDUCE_ONLY)) ? 1024 / NT
+                                      : (Own<Tile, NT>::E == 4 ? (NT <= 256 ? 4 : 1)
                                                               : (NT <= 128 ? 5 : (NT <= 256 ? (REDUCE_ONLY ? 3 : 2) : 1))))
     aw_pass_kernel(const __grid_constant__ AwPassArgs a) {
   extern __shared__ __align__(128) unsigned char aw_smem[];

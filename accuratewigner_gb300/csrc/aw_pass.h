@@ -83,9 +83,14 @@ typedef struct AwPassArgs {
 } AwPassArgs;
 
 // A grouped launch: the passes of up to AW_GROUP_MAX propagators of different line lengths (64 to
-// 2048) run by one persistent kernel, each block walking work items (a member's tile of lines) in
-// index order.  Every member computes with 256 threads of 8 elements a tile (radix-8 stages).
+// AW_GROUP_LONGEST) run by one persistent kernel, each block walking work items (a member's tile of
+// lines) in index order.  Every member computes with AW_GROUP_NT threads of 8 elements a tile of
+// AW_GROUP_TILE elements (radix-8 stages).  Longer members fill the GPU with their own launches and are
+// not grouped (aw_group_propagate runs their own step loop).
 #define AW_GROUP_MAX 8
+#define AW_GROUP_LONGEST 256
+#define AW_GROUP_NT 128
+#define AW_GROUP_TILE 1024
 typedef struct AwGroupArgs {
   int count;
   int start[AW_GROUP_MAX + 1];  // first work item of each member; start[count]: the total

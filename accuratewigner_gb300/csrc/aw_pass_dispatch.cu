@@ -62,4 +62,6 @@ extern "C" int aw_row_pass_blocks(int nrows, int ncols, int f32) {
 }
 extern "C" int aw_col_pass_max_lines(int nrows, int ncols, int f32) { return max_col_lines(nrows, ncols, f32 ? 8 : 16); }
 // lines of a grouped pass's tile (aw_group.cuh: 2048 elements)
-extern "C" int aw_group_tile_lines(int n) { return (n >= 64 && n <= 2048 && !(n & (n - 1))) ? 2048 / n : 0; }
+extern "C" int aw_group_tile_lines(int n) {
+  return (n >= 64 && n <= AW_GROUP_LONGEST && !(n & (n - 1))) ? AW_GROUP_TILE / n : 0;
+}

@@ -522,7 +522,8 @@ def run_plain(args):
              precision=args.precision)
     g = WignerMoyalCUDA1D(**p)
     g.set_wignerfunction("exp(-pow(X - 1., 2) - P * P) / M_PI")
-    g.propagate(20)
+    for _ in range(2):  # warm-up calls of the timed length (their step-window graphs are captured here)
+        g.propagate(CHUNK)
     steps = 1000
     with ClockSampler(0) as clk:
         sec, _ = _timed(lambda: [g.propagate(CHUNK) for _ in range(steps // CHUNK)])
@@ -735,45 +736,66 @@ def run_frames(args):
            "clocks": clk.summary()})
 
 
+def _group_sets(spec):
+    """'128,256,512;128x8' -> [[128, 256, 512], [128] * 8]"""
+    out = []
+    for part in spec.split(";"):
+        sides = []
+        for tok in part.split(","):
+            n, _, k = tok.strip().partition("x")
+            sides += [int(n)] * (int(k) if k else 1)
+        out.append(sides)
+    return out
+
+
 def run_group(args):
-    """Von Neumann propagators of sides 128, 256, 512, 1024 and 2048 (one each, their own potentials),
-    200 steps: grouped (one persistent launch per pass of a step for all five) against the same
-    propagators stepped one after another through propagate()."""
+    """Von Neumann propagators of the given sides (default one each of 128, 256, 512, 1024 and 2048; their
+    own potentials), 200 steps: grouped (one persistent launch per pass of a step for all of them) against
+    the same propagators stepped one after another through propagate().  One line per set of sides."""
     import torch
 
     from accuratewigner_gb300 import RhoVNeumannCUDA1D
     from accuratewigner_gb300.batch import propagate_group
 
-    sides = [128, 256, 512, 1024, 2048]
     steps = 200
     init = ("exp(-0.5 * pow(X - x0, 2) - 0.5 * pow(X_prime - x0, 2)) * "
             "exp(cuda_complex(0., p0) * (X - X_prime))")
 
-    def make():
-        out = []
+    for sides in _group_sets(args.sides):
+        props = []
         for k, n in enumerate(sides):
             a = float(np.sqrt(np.pi * n / 2.0))
             g = RhoVNeumannCUDA1D(t=0.0, dt=0.01, X_gridDIM=n, X_amplitude=a, x0=0.3 * k, p0=-0.2 * k,
                                   c2=0.2 + 0.1 * k, K="0.5 * P * P", V="c2 * X * X + 0.01 * X * X * X * X",
                                   precision=args.precision)
             g.set_rho(init)
-            out.append(g)
-        return out
+            props.append(g)
+        work = float(sum(n * n for n in sides)) * steps
+        # warm-up calls of the timed length (step-window graphs are captured per call length)
+        for _ in range(2):
+            propagate_group(props, CHUNK)
+        with ClockSampler(0) as clk:
+            t_group, _ = _timed(lambda: [propagate_group(props, CHUNK) for _ in range(steps // CHUNK)])
+        for _ in range(2):
+            for g in props:
+                g.propagate(CHUNK)
+        # each member through its own propagate(); the members' streams overlap on the device
+        t_streams, _ = _timed(lambda: [[g.propagate(CHUNK) for g in props] for _ in range(steps // CHUNK)])
 
-    work = float(sum(n * n for n in sides)) * steps
-    props = make()
-    propagate_group(props, 3)  # warm-up
-    with ClockSampler(0) as clk:
-        t_group, _ = _timed(lambda: [propagate_group(props, CHUNK) for _ in range(steps // CHUNK)])
-    for g in props:
-        g.propagate(3)
-    t_seq, _ = _timed(lambda: [[g.propagate(CHUNK) for g in props] for _ in range(steps // CHUNK)])
-    for g in props:
-        g.close()
-    _line("group", "grid-pt*steps/s (five von Neumann propagators of sides 128-2048 stepped as one group)",
-          work / t_group, "grid-pt*steps/s", t_group, args,
-          {"sides": sides, "steps": steps, "steps_per_call": CHUNK, "precision": args.precision},
-          {"one_after_another": work / t_seq, "speedup": t_seq / t_group, "clocks": clk.summary()})
+        def serial():
+            for _ in range(steps // CHUNK):
+                for g in props:
+                    g.propagate(CHUNK)
+                    torch.cuda.synchronize()
+
+        t_serial, _ = _timed(serial)  # one member at a time
+        for g in props:
+            g.close()
+        _line("group", "grid-pt*steps/s (von Neumann propagators of sides %s stepped as one group)"
+              % ",".join(map(str, sides)), work / t_group, "grid-pt*steps/s", t_group, args,
+              {"sides": sides, "steps": steps, "steps_per_call": CHUNK, "precision": args.precision},
+              {"own_streams": work / t_streams, "vs_own_streams": t_streams / t_group,
+               "one_at_a_time": work / t_serial, "vs_one_at_a_time": t_serial / t_group, "clocks": clk.summary()})
 
 
 def large_vn_config(n=4096):
@@ -882,6 +904,8 @@ def main():
     ap.add_argument("--requests", type=int, default=60, help="served: number of requests (per rate for the sweep)")
     ap.add_argument("--rate", type=float, default=4.0, help="served: Poisson arrival rate per second")
     ap.add_argument("--rates", default="1,1.5,2,3,4", help="served-sweep: comma-separated arrival rates per second")
+    ap.add_argument("--sides", default="128,256,512,1024,2048",
+                    help="group: sets of grid sides separated by ';', each a comma list ('NxK' = K members of side N)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

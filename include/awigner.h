@@ -173,15 +173,18 @@ int aw_graph(aw_handle h, int32_t enable);
  * propagator per script): `steps` real-time steps of `count` (1 to 8) von
  * Neumann handles of different square grid sizes (sides 64 to 2048, powers of
  * two; each handle a single propagator or a batch, over its current view), as
- * aw_propagate does for each (rho_vneumann_cuda_1d.py:429-448), with every pass
- * of a step ONE persistent launch over the tiles of all of them and the trace
- * normalisation one launch over all their instances.  Members must share one
+ * aw_propagate does for each (rho_vneumann_cuda_1d.py:429-448).  Members of
+ * side up to 128 (complex64: 256) step together: every pass of a step is ONE
+ * persistent launch over the tiles of all of them and the trace normalisation
+ * one launch over all their instances; they compute with 8 elements a thread
+ * (radix-8 FFT stages) in both passes, give the same bits alone (a group of
+ * one) as in any group, and agree with their own aw_propagate with those
+ * shapes (aw_pass_form) to rounding.  That work runs on the first grouped
+ * member's stream; each grouped member's stream waits for it.  Larger members
+ * fill the GPU with their own launches: each runs aw_propagate's step loop
+ * (its bits) on its own stream, concurrently.  Members must share one
  * arithmetic form and record no per-step observables; V, K and absorbers must
- * not depend on t.  t[k] is member k's time, advanced on return.  Every member
- * computes with 8 elements a thread (radix-8 FFT stages) in both passes and
- * gives the same bits alone (a group of one) as in any group; against its own
- * aw_propagate with those shapes (aw_pass_form) it agrees to rounding.  The work
- * runs on the first member's stream; each member's stream waits for it. */
+ * not depend on t.  t[k] is member k's time, advanced on return. */
 int aw_group_propagate(aw_handle* handles, int32_t count, int64_t steps, double* t);
 
 #define AW_PROF_CLASSES 5

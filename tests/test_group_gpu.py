@@ -1,10 +1,12 @@
 """Grouped propagation: von Neumann propagators of different grid sizes, and a batch, advanced together
-with one persistent launch per pass of a step (aw_group_propagate).
+(aw_group_propagate): members of side up to 128 (complex64: 256) with one persistent launch per pass of a
+step, larger ones through their own step loop on their own streams, concurrently.
 
 * A member computes the same bits alone (a group of one) and in a group with others: its tiles run the
   same kernel code whichever other members share the launch.
 * The grouped steps agree with the member's ordinary propagate() (rho_vneumann_cuda_1d.py:429-448, held
-  to the oracle elsewhere) to rounding: both use radix-8 stages, in separately compiled kernels.
+  to the oracle elsewhere) to rounding: both use radix-8 stages, in separately compiled kernels.  A
+  larger member gives propagate()'s bits.
 """
 import ctypes
 
@@ -18,6 +20,11 @@ pytestmark = pytest.mark.gpu
 INIT = ("exp(-sigma * pow(X - x0, 2) + cuda_complex(0., p0) * X) * "
         "exp(-sigma * pow(X_prime - x0, 2) - cuda_complex(0., p0) * X_prime)")
 ROUNDING = {"c128": 1e-12, "c128-fp64": 1e-12, "c64": 1e-5}
+
+
+def _own(n, precision):
+    """True when a member of side n runs its own step loop instead of the grouped launches."""
+    return n > (256 if precision == "c64" else 128)
 
 
 def _params(n, k, precision):
@@ -39,7 +46,7 @@ def test_group_of_sizes_alone_in_the_mix_and_against_propagate(precision):
     from accuratewigner_gb300 import RhoVNeumannCUDA1D
     from accuratewigner_gb300.batch import propagate_group
 
-    sizes = [64, 256, 1024, 2048]
+    sizes = [64, 128, 256, 1024]
     steps = 7
 
     def fresh(k, n):
@@ -61,6 +68,13 @@ def test_group_of_sizes_alone_in_the_mix_and_against_propagate(precision):
         assert float(g.t) == mixed[k][1]
         assert np.array_equal(g.rho.get(), mixed[k][0]), n
         g.close()
+        if _own(n, precision):
+            # a large member runs its own step loop: propagate()'s bits
+            g = fresh(k, n)
+            g.propagate(3)
+            g.propagate(steps - 3)
+            assert np.array_equal(g.rho.get(), mixed[k][0]), n
+            g.close()
         # the ordinary step loop with the same radix: the same to rounding
         g = fresh(k, n)
         _radix8(g, n, precision)
