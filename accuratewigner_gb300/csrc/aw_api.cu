@@ -222,8 +222,7 @@ struct aw_state_s {
   int z_cluster = 1;                   // ... and blocks per cluster
   DevBuf blk_tabs;                     // Blackman tables
   int shx_lo_n = 0, shy_lo_n = 0;
-  DevBuf twist_hi, twist_lo;           // von Neumann momentum-diagonal twist exp(2 pi i k i / N) / N
-  int twist_lo_n = 0;
+  DevBuf gdiag;                        // von Neumann: diagonal sums G_d of the branch point, then DFT scratch
   int sw_rows = 1;                     // Schrodinger: rows of the zero-padded psi tile
   // Schrodinger wave functions longer than one pass tile: psi read as an sw_n1 x sw_n2 matrix and
   // transformed by the four-step FFT (sw_run); 0 for the single-tile form
@@ -534,31 +533,6 @@ static int make_shear(DevBuf& hi, DevBuf& lo, int* lo_n, const std::vector<doubl
 }
 
 // exp(2 pi i (line * q mod n) / n) / n split as hi[q / lo] * lo[q % lo], exact integer reduction
-static int make_twist(DevBuf& hi, DevBuf& lo, int* lo_n, int n, int fmt) {
-  const int LO = n < 32 ? n : 32;
-  const int nhi = n / LO;
-  const long double PI = 3.141592653589793238462643383279502884L;
-  std::vector<double> H(2 * (size_t)n * nhi), L(2 * (size_t)n * LO);
-  for (long long ln = 0; ln < n; ++ln) {
-    for (int h = 0; h < nhi; ++h) {
-      const long long m = (ln * (long long)(h * LO)) % n;
-      const long double a = 2.0L * PI * (long double)m / (long double)n;
-      H[2 * ((size_t)ln * nhi + h)] = (double)(cosl(a) / n);
-      H[2 * ((size_t)ln * nhi + h) + 1] = (double)(sinl(a) / n);
-    }
-    for (int l = 0; l < LO; ++l) {
-      const long long m = (ln * (long long)l) % n;
-      const long double a = 2.0L * PI * (long double)m / (long double)n;
-      L[2 * ((size_t)ln * LO + l)] = (double)cosl(a);
-      L[2 * ((size_t)ln * LO + l) + 1] = (double)sinl(a);
-    }
-  }
-  TRY(upload_reals(hi, H, fmt));
-  TRY(upload_reals(lo, L, fmt));
-  *lo_n = LO;
-  return AW_OK;
-}
-
 // exp(sign 2 pi i (line * q mod modulus) / modulus) for lines x npos, split as hi[q / lo] * lo[q % lo]
 // (the four-step FFT's twiddles: line = n2, q = k1, modulus = N), exact integer reduction
 static int make_twist4(DevBuf& hi, DevBuf& lo, int* lo_n, int lines, int npos, long long modulus, int sign, int fmt) {
@@ -1290,7 +1264,7 @@ static int create_impl(const aw_config* cfg, aw_state_s* h, bool check_only = fa
     TRY(make_shear(h->shy_hi, h->shy_lo, &h->shy_lo_n, ay, M, 1.0 / M, tab_fmt(h)));
   }
 
-  if (h->kn.vn) TRY(make_twist(h->twist_hi, h->twist_lo, &h->twist_lo_n, h->nc, tab_fmt(h)));
+  if (h->kn.vn) TRY(dalloc(h->gdiag, 2 * (size_t)h->nc * 16));
 
   // reduction scratch of the Wigner column pass
   const int wr = h->kn.rotated ? h->nr : (h->wn ? h->wn : 32), wc = h->kn.rotated ? h->nc : (h->wn ? h->wn : 32);
@@ -1375,7 +1349,7 @@ extern "C" int aw_destroy(aw_handle h) {
   if (!h) return AW_OK;
   if (h->st) cudaStreamSynchronize(h->st);
   DevBuf* bufs[] = {&h->tw_l1, &h->tw_l2, &h->swf_hi, &h->swf_lo, &h->swi_hi, &h->swi_lo,
-                    &h->vseq, &h->vtimes, &h->zbuf, &h->altbuf, &h->twist_hi, &h->twist_lo, &h->rho, &h->W, &h->snap, &h->tmp, &h->stage, &h->tw_r, &h->tw_c, &h->tw_w, &h->shx_hi,
+                    &h->vseq, &h->vtimes, &h->zbuf, &h->altbuf, &h->gdiag, &h->rho, &h->W, &h->snap, &h->tmp, &h->stage, &h->tw_r, &h->tw_c, &h->tw_w, &h->shx_hi,
                     &h->shx_lo, &h->shy_hi, &h->shy_lo, &h->tabs, &h->maskx, &h->maskp, &h->red_line,
                     &h->red_cross, &h->red_sq, &h->rowsum, &h->diag, &h->abs2, &h->scal, &h->stop, &h->hist,
                     &h->terms, &h->part, &h->blk_tabs, &h->params, &h->bvec, &h->maskx2, &h->masksep,
@@ -2608,7 +2582,11 @@ static int vn_tables(aw_state_s* h, const VnPlan& p, double tn, bool kfirst) {
 }
 
 // momentum-space diagonal of rho_n:  M_k = (1/N) Sum_i [fft1(S rho_n)]_ik exp(+2 pi i k i / N),
-// so that Tr[g(p) rho] dX = Sum_k g(P_k) M_k dX (the p branch of get_average, vn:548-561)
+// so that Tr[g(p) rho] dX = Sum_k g(P_k) M_k dX (the p branch of get_average, vn:548-561).  With
+// d = j - i the double sum is a DFT of the diagonal sums of S rho_n:
+//   M_k = (1/N) Sum_d G_d exp(-2 pi i k d / N),   G_d = Sum_i (S rho_n)_{i, (i + d) mod N},
+// so the row pass stores its branch point rotated (no transform), a column pass adds the diagonals and
+// one N-point DFT a step gives M (aw_k_diag_dft).
 //   hist: the first instance's rows (hist_stride values apart), instances inst_stride values apart
 static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::vector<double>& times, double* hist,
                   int hist_stride, long long inst_stride = 0) {
@@ -2672,13 +2650,10 @@ static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::ve
         a.mid_sign = 1;
       }
       if (p.observables) {
+        // the branch point, each row i rotated left by i and signed (-1)^i: its alternating column
+        // sums are the diagonal sums G_d (below)
         a.br_out = h->tmp.p;
-        a.br_d1 = +1;
-        a.fbr = fnone();
-        a.fbr.sh_hi = h->twist_hi.p;
-        a.fbr.sh_lo = h->twist_lo.p;
-        a.fbr.sh_lo_n = h->twist_lo_n;
-        a.fbr.active = 1;
+        a.br_rot = 1;
       }
       if (!last) {
         a.f2 = ftab(h, vdep ? TAB_V1B : vslot);
@@ -2691,12 +2666,15 @@ static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::ve
     }
     double* hrow = hist ? hist + (size_t)(n - 1) * hist_stride : nullptr;
     if (p.observables) {
-      // column sums of the twisted branch: Re M_k
+      // G_d = Sum_i (S rho)_{i, i+d} (alternating column sums of the rotated branch), then
+      // Re M_k = Re (1/N) Sum_d G_d exp(-2 pi i k d / N) into red_line
       AwPassArgs a = pnone(h);
       a.in = h->tmp.p;
-      a.red_line = (double*)h->red_line.p;
+      a.col_alt = (double2*)h->gdiag.p;
       a.stop = stop;
       TRY(col_pass(h, a, h->tw_c));
+      KL(aw_k_diag_dft((const double2*)h->gdiag.p, N, (double2*)h->gdiag.p + N, (double*)h->red_line.p, 1.0 / N,
+                       h->st));
     }
     if (p.bloch || !p.observables) {
       KL(aw_k_trace_finalize_n((const double2*)h->diag.p + (size_t)h->v0 * N,

@@ -149,6 +149,21 @@ __device__ __forceinline__ void store_regs(V* __restrict__ dst, const V* r, int 
   }
 }
 
+// the branch store of a row tile rotated: element (lg, pos) to (lg, (pos - lg) mod N), times (-1)^lg
+template <typename V, class Tile, int NT>
+__device__ __forceinline__ void store_regs_rot(V* __restrict__ dst, const V* r, int lg, int pos0, int ncols) {
+  constexpr int E = Own<Tile, NT>::E;
+  constexpr int STEP = Own<Tile, NT>::STEP;
+  static_assert(Tile::IS_ROW, "rotated stores are row-tile stores");
+#pragma unroll
+  for (int k = 0; k < E; ++k) {
+    const int pos = pos0 + k * STEP;
+    V v = r[k];
+    if (lg & 1) v = cflip(v, 0x80000000u);
+    dst[(long long)lg * ncols + ((pos - lg) & (Tile::N - 1))] = v;
+  }
+}
+
 // deterministic block sum of one double per thread (NT a power of two); result valid in thread 0:
 // a fixed shuffle tree inside each warp, then the warp sums in index order (two barriers instead of
 // one per halving)
@@ -291,7 +306,12 @@ __device__ __forceinline__ void aw_pass_body(const AwPassArgs& a, const int bx, 
       }
     }
     if (seg == 2) {
-      store_regs<V, Tile, NT>((V*)a.br_out + eoff, r, lg, pos0, ncols, false);
+      if constexpr (Tile::IS_ROW) {
+        if (a.br_rot)
+          store_regs_rot<V, Tile, NT>((V*)a.br_out + eoff, r, lg, pos0, ncols);
+        else
+          store_regs<V, Tile, NT>((V*)a.br_out + eoff, r, lg, pos0, ncols, false);
+      }
 #pragma unroll
       for (int k = 0; k < E; ++k) r[k] = keep[k];
     }

@@ -51,6 +51,8 @@ typedef struct AwPassArgs {
   void* mid_out;            // optional store of the tile at the branch point
   int mid_sign;             // ... multiplied by (-1)^(i+j)
   void* br_out;             // optional branch output
+  int br_rot;               // row pass: br_out takes element (i, j) at (i, (j - i) mod ncols), times (-1)^i
+                            // (a column pass's alternating sums of it are the tile's diagonal sums)
   int br_d1;
   AwFactor fbr;
   int br_d2;

@@ -259,6 +259,60 @@ __global__ void k_shear_full(const double2* hi, const double2* lo, int lo_n, int
   }
 }
 
+// The von Neumann momentum diagonal from the diagonal sums G of the branch point (aw_api.cu, vn_run):
+// Re M_k = scale Re Sum_d G_d exp(-2 pi i k d / N), N = n1 n2, in two launches of direct FP64 DFTs
+// (the four-step factorisation, d = d1 + n1 d2, k = k2 + n2 k1):
+//   X[d1][k2] = exp(-2 pi i k2 d1 / N) Sum_d2 G[d1 + n1 d2] exp(-2 pi i k2 d2 / n2)     (block d1)
+//   M[k2 + n2 k1] = scale Sum_d1 X[d1][k2] exp(-2 pi i k1 d1 / n1)                     (block k2)
+// Twiddles from sincospi of exactly reduced integer ratios.
+__global__ void k_diag_dft_a(const double2* g, int n1, int n2, double2* x) {
+  extern __shared__ double2 aw_dsh[];
+  double2* v = aw_dsh;
+  double2* w = aw_dsh + n2;
+  const int d1 = blockIdx.x;
+  for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+    v[t] = g[d1 + (long long)n1 * t];
+    double sn, cs;
+    sincospi(2.0 * t / n2, &sn, &cs);
+    w[t] = make_double2(cs, -sn);
+  }
+  __syncthreads();
+  const long long n = (long long)n1 * n2;
+  for (int k2 = threadIdx.x; k2 < n2; k2 += blockDim.x) {
+    double re = 0.0, im = 0.0;
+    for (int d2 = 0; d2 < n2; ++d2) {
+      const double2 a = v[d2], b = w[(k2 * d2) & (n2 - 1)];
+      re += a.x * b.x - a.y * b.y;
+      im += a.x * b.y + a.y * b.x;
+    }
+    double sn, cs;
+    sincospi(2.0 * (double)(((long long)k2 * d1) % n) / (double)n, &sn, &cs);
+    x[(long long)d1 * n2 + k2] = make_double2(re * cs + im * sn, im * cs - re * sn);
+  }
+}
+
+__global__ void k_diag_dft_b(const double2* x, int n1, int n2, double scale, double* out_re) {
+  extern __shared__ double2 aw_dsh[];
+  double2* v = aw_dsh;
+  double2* w = aw_dsh + n1;
+  const int k2 = blockIdx.x;
+  for (int t = threadIdx.x; t < n1; t += blockDim.x) {
+    v[t] = x[(long long)t * n2 + k2];
+    double sn, cs;
+    sincospi(2.0 * t / n1, &sn, &cs);
+    w[t] = make_double2(cs, -sn);
+  }
+  __syncthreads();
+  for (int k1 = threadIdx.x; k1 < n1; k1 += blockDim.x) {
+    double re = 0.0;
+    for (int d1 = 0; d1 < n1; ++d1) {
+      const double2 a = v[d1], b = w[(k1 * d1) & (n1 - 1)];
+      re += a.x * b.x - a.y * b.y;
+    }
+    out_re[k2 + (long long)n2 * k1] = scale * re;
+  }
+}
+
 __global__ void k_set2(double* p, double a, double b) {
   p[0] = a;
   p[1] = b;
@@ -327,6 +381,16 @@ int aw_k_trace_finalize_n(const double2* diag, int n, const double* abs2part, in
                           void* s) {
   k_trace_finalize<<<ninst, 256, 0, (cudaStream_t)s>>>(diag, n, abs2part, nparts, dX, complex_trace, inv_out, hist,
                                                        hstride, stop, stop_on_purity);
+  return ok();
+}
+int aw_k_diag_dft(const double2* g, int n, double2* scratch, double* out_re, double scale, void* s) {
+  int l = 0;
+  while ((1 << l) < n) ++l;
+  if (n < 1 || (1 << l) != n) return -1;
+  const int n1 = 1 << (l / 2), n2 = n / n1;
+  k_diag_dft_a<<<n1, n2 < 256 ? n2 : 256, 2 * n2 * sizeof(double2), (cudaStream_t)s>>>(g, n1, n2, scratch);
+  k_diag_dft_b<<<n2, n1 < 256 ? n1 : 256, 2 * n1 * sizeof(double2), (cudaStream_t)s>>>(scratch, n1, n2, scale,
+                                                                                       out_re);
   return ok();
 }
 int aw_k_trace_finalize_group(const AwTraceGroup* g, void* s) {

@@ -24,6 +24,8 @@ int aw_k_trace_finalize_n(const double2* diag, int n, const double* abs2part, in
                           double* inv_out, double* hist, long long hstride, int* stop, int stop_on_purity, int ninst,
                           void* s);
 int aw_k_set2(double* p, double a, double b, void* s);
+// Re M_k = scale Re Sum_d g_d exp(-2 pi i k d / n) for k < n (n a power of two; scratch: n complex)
+int aw_k_diag_dft(const double2* g, int n, double2* scratch, double* out_re, double scale, void* s);
 // 1 / trace of every instance of up to 8 propagators (the grouped von Neumann step), member by member
 typedef struct AwTraceGroup {
   int count, complex_trace;

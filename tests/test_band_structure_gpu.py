@@ -36,9 +36,12 @@ def test_ground_state_is_the_lowest_band_and_stays_put():
     r = r / np.trace(r)
     q = lattice(256)
     # splitting error of the imaginary-time step that the dbeta halvings ended on (3e-9 in the FP64
-    # oracle, 2e-8 with double-float passes, whose purity test stops at another step)
+    # oracle, 2e-8 with double-float passes, whose purity test stops at another step).  The search
+    # (rb:163-223) halves dbeta whenever an energy fails to decrease, and near convergence those
+    # comparisons are decided by rounding: where it stops moves the energy by up to 1.5e-8 between
+    # summation orders of the same observables.
     assert np.linalg.norm(r - q.get_gibbs(0.0, 0.5, n=1)) < 1e-7
-    assert abs(q.get_energy(r) - mathieu_levels(False, 1)[0]) < 1e-8
+    assert abs(q.get_energy(r) - mathieu_levels(False, 1)[0]) < 3e-8
     # a stationary state: real-time propagation leaves it in place (bsg:190-192), up to the
     # splitting error of the real-time step (the exact band state drifts by 1.8e-6 over these 200
     # steps of dt = 0.01 in the FP64 oracle)

@@ -11,6 +11,10 @@ by the two engines.
                        absorber on the outer 10 % of x, dt 0.05, 100 steps
   large von Neumann    4096 x 4096, X_amplitude 80, driven Morse potential, dt 0.02, 2 steps with
                        Ehrenfest observables (rho_vneumann_cuda_1d.py:429-448)
+  batched Gibbs        Wigner-Bloch batch on 512 x 512, X_amplitude 10, P_amplitude 8, V = a x^4 - b x^2,
+                       dbeta 0.01: the two highest-temperature of the benchmark's 64 seeded instances
+                       (52 and 59 steps), in both complex128 engines at 1e-10 and in complex64 (purity and
+                       energy against the oracle; wigner_bloch_cuda_1d.py:95-155)
   complex64            the plain Wigner-Moyal run in complex64: Wigner relative L2 error after 1000
                        steps against the bound 1e-5
 """
@@ -119,6 +123,70 @@ def _oracle_vn4096():
     o.set_rho(vn4096_rho0())
     o.propagate(VN4096_STEPS)
     return o.rho.copy(), {k: np.array(getattr(o, k)) for k in NAMES}, o.get_purity()
+
+
+C3 = dict(t=0.0, X_gridDIM=512, P_gridDIM=512, X_amplitude=10.0, P_amplitude=8.0, K="0.5 * P * P",
+          V="a * X * X * X * X - b * X * X", dt=0.01, dbeta=0.01, t_initial=0.0)
+
+
+def c3_instances(count):
+    """(a, b, kT) of the batched Gibbs benchmark's 64 instances (seed 0, drawn as bench.py draws them),
+    the `count` of highest temperature, in increasing step count."""
+    rng = np.random.default_rng(0)
+    a = rng.uniform(0.02, 0.1, 64)
+    b = rng.uniform(0.2, 1.0, 64)
+    beta = np.exp(rng.uniform(np.log(0.5), np.log(20.0), 64))
+    return [(float(a[k]), float(b[k]), float(1.0 / beta[k])) for k in np.argsort(beta, kind="stable")[:count]]
+
+
+@functools.lru_cache(maxsize=None)
+def _oracle_c3():
+    from oracle.propagators import WignerBlochOracle
+
+    out = []
+    for a, b, kT in c3_instances(2):
+        o = WignerBlochOracle(a=a, b=b, kT=kT, **C3)
+        o.get_gibbs_state()
+        out.append((o.wignerfunction.copy(), o.get_purity(), float(o.get_average(o.hamiltonian)),
+                    o.gibbs_steps_done))
+    return tuple(out)
+
+
+def _c3_batch(**kw):
+    from accuratewigner_gb300 import WignerBlochCUDA1D
+    from accuratewigner_gb300.batch import PropagatorBatch
+
+    inst = c3_instances(2)
+    bt = PropagatorBatch(WignerBlochCUDA1D, len(inst), params=("a", "b"), init="1.", kT=1.0, **C3, **kw)
+    for k, (a, b, _) in enumerate(inst):
+        bt.set_params(k, [a, b])
+    done, pur = bt.gibbs([kT for _, _, kT in inst])
+    out = (list(done), list(pur), bt.energy.copy(), [bt.wigner(k) for k in range(len(inst))])
+    bt.close()
+    return out
+
+
+@pytest.mark.usefixtures("c128_engine")
+def test_batched_gibbs_512_against_oracle():
+    done, pur, energy, W = _c3_batch()
+    for k, (Wc, pc, ec, nc) in enumerate(_oracle_c3()):
+        assert done[k] == nc, k
+        assert rel_l2(W[k], Wc) < TOL, k
+        assert abs(pur[k] - pc) < TOL, k
+        assert abs(energy[k] - ec) < TOL * abs(ec), k
+
+
+def test_complex64_batched_gibbs_512_purity_and_energy():
+    """complex64 bulk with FP64 renormalisation against the FP64 oracle.  Bounds: the largest errors
+    against complex128 over the whole 64-instance benchmark batch (up to 2000 steps): purity 8.1e-6,
+    energy 3.0e-5 relative."""
+    done, pur, energy, W = _c3_batch(precision="c64")
+    for k, (Wc, pc, ec, nc) in enumerate(_oracle_c3()):
+        print("complex64 Gibbs instance %d: W %.2e, purity %.2e, energy %.2e" %
+              (k, rel_l2(W[k], Wc), abs(pur[k] - pc), abs(energy[k] - ec) / abs(ec)))
+        assert done[k] == nc, k
+        assert abs(pur[k] - pc) < 8.1e-6, k
+        assert abs(energy[k] - ec) < 3.0e-5 * abs(ec), k
 
 
 @pytest.mark.usefixtures("c128_engine")
