@@ -264,11 +264,14 @@ __global__ void k_shear_full(const double2* hi, const double2* lo, int lo_n, int
 // (the four-step factorisation, d = d1 + n1 d2, k = k2 + n2 k1):
 //   X[d1][k2] = exp(-2 pi i k2 d1 / N) Sum_d2 G[d1 + n1 d2] exp(-2 pi i k2 d2 / n2)     (block d1)
 //   M[k2 + n2 k1] = scale Sum_d1 X[d1][k2] exp(-2 pi i k1 d1 / n1)                     (block k2)
-// Twiddles from sincospi of exactly reduced integer ratios.
+// Twiddles from sincospi of exactly reduced integer ratios.  AW_DFT_PARTS threads share each output
+// (interleaved terms, added in part order), so that the FP64 sums are short chains over more warps.
+#define AW_DFT_PARTS 4
 __global__ void k_diag_dft_a(const double2* g, int n1, int n2, double2* x) {
   extern __shared__ double2 aw_dsh[];
   double2* v = aw_dsh;
   double2* w = aw_dsh + n2;
+  double2* part = aw_dsh + 2 * n2;  // [AW_DFT_PARTS][n2]
   const int d1 = blockIdx.x;
   for (int t = threadIdx.x; t < n2; t += blockDim.x) {
     v[t] = g[d1 + (long long)n1 * t];
@@ -277,13 +280,23 @@ __global__ void k_diag_dft_a(const double2* g, int n1, int n2, double2* x) {
     w[t] = make_double2(cs, -sn);
   }
   __syncthreads();
-  const long long n = (long long)n1 * n2;
-  for (int k2 = threadIdx.x; k2 < n2; k2 += blockDim.x) {
+  for (int u = threadIdx.x; u < n2 * AW_DFT_PARTS; u += blockDim.x) {
+    const int k2 = u % n2, q = u / n2;
     double re = 0.0, im = 0.0;
-    for (int d2 = 0; d2 < n2; ++d2) {
+    for (int d2 = q; d2 < n2; d2 += AW_DFT_PARTS) {
       const double2 a = v[d2], b = w[(k2 * d2) & (n2 - 1)];
       re += a.x * b.x - a.y * b.y;
       im += a.x * b.y + a.y * b.x;
+    }
+    part[q * n2 + k2] = make_double2(re, im);
+  }
+  __syncthreads();
+  const long long n = (long long)n1 * n2;
+  for (int k2 = threadIdx.x; k2 < n2; k2 += blockDim.x) {
+    double re = 0.0, im = 0.0;
+    for (int q = 0; q < AW_DFT_PARTS; ++q) {
+      re += part[q * n2 + k2].x;
+      im += part[q * n2 + k2].y;
     }
     double sn, cs;
     sincospi(2.0 * (double)(((long long)k2 * d1) % n) / (double)n, &sn, &cs);
@@ -295,6 +308,7 @@ __global__ void k_diag_dft_b(const double2* x, int n1, int n2, double scale, dou
   extern __shared__ double2 aw_dsh[];
   double2* v = aw_dsh;
   double2* w = aw_dsh + n1;
+  double* part = reinterpret_cast<double*>(aw_dsh + 2 * n1);  // [AW_DFT_PARTS][n1]
   const int k2 = blockIdx.x;
   for (int t = threadIdx.x; t < n1; t += blockDim.x) {
     v[t] = x[(long long)t * n2 + k2];
@@ -303,12 +317,19 @@ __global__ void k_diag_dft_b(const double2* x, int n1, int n2, double scale, dou
     w[t] = make_double2(cs, -sn);
   }
   __syncthreads();
-  for (int k1 = threadIdx.x; k1 < n1; k1 += blockDim.x) {
+  for (int u = threadIdx.x; u < n1 * AW_DFT_PARTS; u += blockDim.x) {
+    const int k1 = u % n1, q = u / n1;
     double re = 0.0;
-    for (int d1 = 0; d1 < n1; ++d1) {
+    for (int d1 = q; d1 < n1; d1 += AW_DFT_PARTS) {
       const double2 a = v[d1], b = w[(k1 * d1) & (n1 - 1)];
       re += a.x * b.x - a.y * b.y;
     }
+    part[q * n1 + k1] = re;
+  }
+  __syncthreads();
+  for (int k1 = threadIdx.x; k1 < n1; k1 += blockDim.x) {
+    double re = 0.0;
+    for (int q = 0; q < AW_DFT_PARTS; ++q) re += part[q * n1 + k1];
     out_re[k2 + (long long)n2 * k1] = scale * re;
   }
 }
@@ -388,9 +409,11 @@ int aw_k_diag_dft(const double2* g, int n, double2* scratch, double* out_re, dou
   while ((1 << l) < n) ++l;
   if (n < 1 || (1 << l) != n) return -1;
   const int n1 = 1 << (l / 2), n2 = n / n1;
-  k_diag_dft_a<<<n1, n2 < 256 ? n2 : 256, 2 * n2 * sizeof(double2), (cudaStream_t)s>>>(g, n1, n2, scratch);
-  k_diag_dft_b<<<n2, n1 < 256 ? n1 : 256, 2 * n1 * sizeof(double2), (cudaStream_t)s>>>(scratch, n1, n2, scale,
-                                                                                       out_re);
+  const int ta = n2 * AW_DFT_PARTS < 256 ? n2 * AW_DFT_PARTS : 256;
+  const int tb = n1 * AW_DFT_PARTS < 256 ? n1 * AW_DFT_PARTS : 256;
+  k_diag_dft_a<<<n1, ta, (2 + AW_DFT_PARTS) * n2 * sizeof(double2), (cudaStream_t)s>>>(g, n1, n2, scratch);
+  k_diag_dft_b<<<n2, tb, 2 * n1 * sizeof(double2) + AW_DFT_PARTS * n1 * sizeof(double), (cudaStream_t)s>>>(
+      scratch, n1, n2, scale, out_re);
   return ok();
 }
 int aw_k_trace_finalize_group(const AwTraceGroup* g, void* s) {

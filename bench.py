@@ -618,6 +618,8 @@ def run_served(args):
     eng = Engine(precision=args.precision, chunk=200)
     eng.warm()
     reqs = make_stream(args.requests, args.rate, seed=0)
+    for r in reqs:
+        r.tol = args.tol
     with ClockSampler(0) as clk:
         wall = eng.run(reqs)
     eng.close()
@@ -631,7 +633,7 @@ def run_served(args):
            "steps": "U(100, 5000)", "kinds": ["wigner-moyal (Ehrenfest)", "von Neumann", "rho-Bloch Gibbs"],
            "potential": "c2 x^2 + c3 x^3 + c4 x^4, c2 ~ U(0.1, 1), c3 ~ U(-0.02, 0.02), c4 ~ U(0, 0.05)",
            "amplitude": "X_amplitude = P_amplitude = sqrt(pi N / 2)", "chunk_steps": 200,
-           "precision": args.precision},
+           "precision": args.precision, "tolerance": args.tol},
           dict({"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
                 "mean_latency_s": float(lat.mean()), "p50_latency_by_kind_s": by_kind, "clocks": clk.summary()},
                **auto_summary(reqs)))
@@ -662,6 +664,8 @@ def run_served_sweep(args):
     with ClockSampler(0) as clk:
         for rate in rates:
             reqs = make_stream(args.requests, rate, seed=0)
+            for r in reqs:
+                r.tol = args.tol
             span = max(r.arrival for r in reqs)
             asked = float(sum(r.n * r.n * r.steps for r in reqs))  # rho-Bloch requests may stop early
             wall = eng.run(reqs)
@@ -904,6 +908,8 @@ def main():
     ap.add_argument("--requests", type=int, default=60, help="served: number of requests (per rate for the sweep)")
     ap.add_argument("--rate", type=float, default=4.0, help="served: Poisson arrival rate per second")
     ap.add_argument("--rates", default="1,1.5,2,3,4", help="served-sweep: comma-separated arrival rates per second")
+    ap.add_argument("--tol", type=float, default=1e-5,
+                    help="served: each request's relative error tolerance (precision auto runs complex64 within it)")
     ap.add_argument("--sides", default="128,256,512,1024,2048",
                     help="group: sets of grid sides separated by ';', each a comma list ('NxK' = K members of side N)")
     args = ap.parse_args()
