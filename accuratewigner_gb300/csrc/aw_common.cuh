@@ -165,7 +165,7 @@ template <> __device__ __forceinline__ dfc cscale<dfc>(dfc a, dfr s) { return df
 // sign flips by a mask of the sign bit (0 or 0x80000000), on the integer pipe
 __device__ __forceinline__ float flip(float v, unsigned m) { return __int_as_float(__float_as_int(v) ^ (int)m); }
 __device__ __forceinline__ double flip(double v, unsigned m) {
-  return __hiloint2double(__double2hiint(v) ^ (int)m, __double2loint(v));
+  return __longlong_as_double(__double_as_longlong(v) ^ (long long)((unsigned long long)m << 32));
 }
 __device__ __forceinline__ dfr flip(dfr v, unsigned m) { return dfr{flip(v.h, m), flip(v.l, m)}; }
 __device__ __forceinline__ float2 flip(float2 v, unsigned mx, unsigned my) { return make_float2(flip(v.x, mx), flip(v.y, my)); }

@@ -145,9 +145,14 @@ __device__ __forceinline__ void bf_tan(double2& a, double2& b, double2 mq, int e
   const double q = flip(mq.y, inv);
   e = (inv ? -e : e) & 3;
   const double ux = fma(-q, b.y, b.x), uy = fma(q, b.x, b.y);
-  const bool sw = e & 1;
-  const double vx = flip(sw ? uy : ux, ((e ^ (e >> 1)) & 1) ? 0x80000000u : 0u);
-  const double vy = flip(sw ? ux : uy, (e >> 1) ? 0x80000000u : 0u);
+  // v = i^e u by bit operations on the integer pipe (a swap when e is odd, then sign flips): e varies
+  // across the lanes of a row tile, and a data-dependent select there left FP64 instructions issued
+  // for part of a warp (23.7 of 32 lanes active on average in the headline's row pass)
+  const unsigned long long xb = (unsigned long long)__double_as_longlong(ux);
+  const unsigned long long yb = (unsigned long long)__double_as_longlong(uy);
+  const unsigned long long t = (xb ^ yb) & (0ull - (unsigned long long)(e & 1));
+  const double vx = __longlong_as_double((long long)(xb ^ t ^ ((unsigned long long)((e ^ (e >> 1)) & 1) << 63)));
+  const double vy = __longlong_as_double((long long)(yb ^ t ^ ((unsigned long long)((e >> 1) & 1) << 63)));
   const double m = mq.x;
   const double2 a0 = a;
   a = make_double2(fma(m, vx, a0.x), fma(m, vy, a0.y));

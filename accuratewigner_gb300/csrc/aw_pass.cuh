@@ -108,7 +108,7 @@ __device__ __forceinline__ void apply_factor(V* r, const AwFactor& f, int lg, in
     const int i = Tile::IS_ROW ? lg : pos;
     const int j = Tile::IS_ROW ? pos : lg;
     V v = r[k];
-    if (sgn && ((sgn == 1 ? i + j : (sgn == 2 ? i : j)) & 1)) v = cflip(v, 0x80000000u);
+    if (sgn) v = cflip(v, ((sgn == 1 ? i + j : (sgn == 2 ? i : j)) & 1) ? 0x80000000u : 0u);
     if (mk) {
       T q = mk[(long long)i * ncols + j];
       if (f.mask_pow == 2) q = q * q;
@@ -144,7 +144,7 @@ __device__ __forceinline__ void store_regs(V* __restrict__ dst, const V* r, int 
   for (int k = 0; k < E; ++k) {
     const int pos = pos0 + k * STEP;
     V v = r[k];
-    if (sgn && ((lg + pos) & 1)) v = cflip(v, 0x80000000u);
+    if (sgn) v = cflip(v, ((lg + pos) & 1) ? 0x80000000u : 0u);
     dst[gidx<Tile>(lg, pos, ncols)] = v;
   }
 }
@@ -353,16 +353,14 @@ __device__ __forceinline__ void aw_pass_body(const AwPassArgs& a, const int bx, 
       for (int k = 0; k < E; ++k) {
         const int pos = pos0 + k * STEP;
         const T re = cre(r[k]), im = cim(r[k]);
-        if (pos & 1) {
-          cr -= re;
-          ci -= im;
-        } else {
-          cr += re;
-          ci += im;
-        }
+        // (-1)^pos by a sign-bit flip, not a branch: pos differs across the lanes of a warp
+        const unsigned sp = (pos & 1) ? 0x80000000u : 0u;
+        cr += flip(re, sp);
+        ci += flip(im, sp);
         if (a.alt_cross) {
           // across the block's B columns in working precision (B <= 16 terms), FP64 beyond
-          T xr = (lg & 1) ? -re : re, xi = (lg & 1) ? -im : im;
+          const unsigned sl = (lg & 1) ? 0x80000000u : 0u;
+          T xr = flip(re, sl), xi = flip(im, sl);
 #pragma unroll
           for (int o = B / 2; o > 0; o >>= 1) {
             xr += shfl_xor(lane_mask<NT>(), xr, o, B);
