@@ -327,10 +327,15 @@ __device__ __forceinline__ void aw_pass_body(const AwPassArgs& a, const int bx, 
     if (seg == 0) {
       if (!LEAN && Tile::IS_ROW && a.mid_out) store_regs<V, Tile, NT>((V*)a.mid_out + eoff, r, lg, pos0, ncols, a.mid_sign != 0);
       if (Tile::IS_ROW && a.diag_out) {
+        // the element (lg, lg), when this thread holds it: picked by selects, then one conversion
+        // under a real branch (per-element conditional conversions were predicated FP64 work)
+        const int kd = (lg - pos0) / STEP;
+        if (lg >= pos0 && (lg - pos0) % STEP == 0 && kd < E) {
+          V d = r[0];
 #pragma unroll
-        for (int k = 0; k < E; ++k)
-          if (pos0 + k * STEP == lg)
-            a.diag_out[(long long)inst * a.nrows + lg] = make_double2(to_d(cre(r[k])), to_d(cim(r[k])));
+          for (int k = 1; k < E; ++k) d = k == kd ? r[k] : d;
+          a.diag_out[(long long)inst * a.nrows + lg] = make_double2(to_d(cre(d)), to_d(cim(d)));
+        }
       }
       if (!LEAN && a.red_abs2 && !a.abs2_end) {
         T acc = from_double<T>(0.0);
@@ -383,19 +388,25 @@ __device__ __forceinline__ void aw_pass_body(const AwPassArgs& a, const int bx, 
     // FP64 across threads in a fixed order
     if (a.col_alt || a.alt_cross) {
       __shared__ typename cpart<V>::type cred[NT];
+      // each reduction in its own loop under one uniform branch (no predicated arithmetic, see
+      // apply_factor); every accumulator adds its terms in the same order as before
       T cr = from_double<T>(0.0), ci = from_double<T>(0.0);
+      if (a.col_alt) {
 #pragma unroll
-      for (int k = 0; k < E; ++k) {
-        const int pos = pos0 + k * STEP;
-        const T re = cre(r[k]), im = cim(r[k]);
-        // (-1)^pos by a sign-bit flip, not a branch: pos differs across the lanes of a warp
-        const unsigned sp = (pos & 1) ? 0x80000000u : 0u;
-        cr += flip(re, sp);
-        ci += flip(im, sp);
-        if (a.alt_cross) {
-          // across the block's B columns in working precision (B <= 16 terms), FP64 beyond
-          const unsigned sl = (lg & 1) ? 0x80000000u : 0u;
-          T xr = flip(re, sl), xi = flip(im, sl);
+        for (int k = 0; k < E; ++k) {
+          // (-1)^pos by a sign-bit flip, not a branch: pos differs across the lanes of a warp
+          const unsigned sp = ((pos0 + k * STEP) & 1) ? 0x80000000u : 0u;
+          cr += flip(cre(r[k]), sp);
+          ci += flip(cim(r[k]), sp);
+        }
+      }
+      if (a.alt_cross) {
+        // across the block's B columns in working precision (B <= 16 terms), FP64 beyond
+        const unsigned sl = (lg & 1) ? 0x80000000u : 0u;
+#pragma unroll
+        for (int k = 0; k < E; ++k) {
+          const int pos = pos0 + k * STEP;
+          T xr = flip(cre(r[k]), sl), xi = flip(cim(r[k]), sl);
 #pragma unroll
           for (int o = B / 2; o > 0; o >>= 1) {
             xr += shfl_xor(lane_mask<NT>(), xr, o, B);
@@ -447,20 +458,28 @@ __device__ __forceinline__ void aw_pass_body(const AwPassArgs& a, const int bx, 
     if (a.red_line || a.red_cross || a.red_sq) {
       typedef typename acc_of<V>::type A;
       A lsum = to_acc<A>(0.0), sq = to_acc<A>(0.0);
+      if (a.red_line) {
 #pragma unroll
-      for (int k = 0; k < E; ++k) {
-        const int pos = pos0 + k * STEP;
-        const A re = to_acc<A>(cre(r[k])), im = to_acc<A>(cim(r[k]));
-        lsum += re;
-        sq += re * re - im * im;
-        if (a.red_cross) {
+        for (int k = 0; k < E; ++k) lsum += to_acc<A>(cre(r[k]));
+      }
+      if (a.red_sq) {
+#pragma unroll
+        for (int k = 0; k < E; ++k) {
+          const A re = to_acc<A>(cre(r[k])), im = to_acc<A>(cim(r[k]));
+          sq += re * re - im * im;
+        }
+      }
+      if (a.red_cross) {
+#pragma unroll
+        for (int k = 0; k < E; ++k) {
           // across the block's B columns: FP32 for complex64 (B <= 16 terms), FP64 otherwise
+          const A re = to_acc<A>(cre(r[k]));
           typedef typename std::conditional<std::is_same<A, float>::value, float, double>::type C;
           C c;
           if constexpr (std::is_same<C, float>::value) c = re; else c = to_d(re);
 #pragma unroll
           for (int o = B / 2; o > 0; o >>= 1) c += shfl_xor(lane_mask<NT>(), c, o, B);
-          if (line == 0) a.red_cross[((long long)inst * gx + bx) * a.nrows + pos] = (double)c;
+          if (line == 0) a.red_cross[((long long)inst * gx + bx) * a.nrows + pos0 + k * STEP] = (double)c;
         }
       }
       if (a.red_line) {
