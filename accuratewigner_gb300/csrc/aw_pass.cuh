@@ -29,16 +29,17 @@ namespace cg = cooperative_groups;
 // registers, 4 blocks a SM): more warps for the latency-bound row pass, whose branch point keeps a
 // second copy of the elements in registers (measured: 0.174 -> 0.170 ms a step; tiles of several
 // shorter rows spill at 64 registers and keep 8 elements a thread).
-// Complex64 tiles of 2048 elements and more keep 16 elements a thread (two radix-8 butterflies a thread
-// a stage, half the threads): 4096^2 von Neumann 0.608 -> 0.573 ms a step, the 64 x 512^2 Gibbs batch
-// +2 %, the 1024^2 and 256^2 Wigner-Moyal steps equal.
+// Complex64 tiles of 4096 elements and more keep 16 elements a thread (two radix-8 butterflies a thread
+// a stage, half the threads): 4096^2 von Neumann 0.608 -> 0.573 ms a step.  Smaller tiles keep 8, so
+// that their other shape (4 elements, radix-4 stages) exists at every column width: a width then
+// never changes the radix a grid's tuned shape sets.
 // ALT: the other number of elements a thread (4 where the rule above gives 8, 8 where it gives 4), so
 // the other FFT radix (stages of radix min(8, E)); offered to the autotuner for lines of 256 to 2048
 // points where the block stays within 512 threads (ALT_OK).
 template <typename V, int N, int LINES, bool ROW = false, bool ALT = false> struct Shape {
   static constexpr int TILE = N * LINES;
   static constexpr int E0 = (ROW && std::is_same<V, dfc>::value && N == 1024 && LINES == 1) ? 4
-                            : ((std::is_same<V, float2>::value && TILE >= 2048) ? (TILE / 512 > 16 ? TILE / 512 : 16)
+                            : ((std::is_same<V, float2>::value && TILE >= 4096) ? (TILE / 512 > 16 ? TILE / 512 : 16)
                                                                                   : (TILE / 512 > 8 ? TILE / 512 : 8));
   static constexpr int E1 = E0 == 4 ? 8 : (E0 == 8 ? 4 : E0);
   static constexpr bool ALT_OK = N >= 256 && N <= 2048 && E1 != E0 && TILE / E1 <= 512 && TILE % E1 == 0;
