@@ -157,15 +157,17 @@ class TermTable:
         cfg.obs_p_time_dependent = int(any(self.info.depends_on(e, "t") for e in self.obs_p))
 
 
-# precision of propagators constructed without the keyword
-DEFAULT_PRECISION = "c128"
+# precision of propagators constructed without the keyword: the reference's own arithmetic
+# (pycuda::complex<double>, wigner_moyal_cuda_1d.py:629)
+DEFAULT_PRECISION = "c128-fp64"
 
 
 def precision_code(kwargs):
     """State and arithmetic of the passes.
 
-    'c128' (default): complex128 state, passes in double-float arithmetic on the FP32 pipes.
-    'c128-fp64': complex128 state, passes in native FP64 arithmetic.
+    'c128-fp64' (default): complex128 state, passes in native FP64 arithmetic.
+    'c128': complex128 state, passes in double-float arithmetic on the FP32 pipes (about 1e-13 from
+            FP64, values below about 1e-30 lose their low part; about 3x faster).
     'c64': complex64 state and passes, FP64 tables and reductions.
     """
     p = kwargs.get("precision", DEFAULT_PRECISION)

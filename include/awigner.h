@@ -43,7 +43,8 @@ extern "C" {
 #define AW_C128 0           /* complex128 state, as the reference (wigner_moyal_cuda_1d.py:629); passes in
                                double-float arithmetic (FP32 hi + lo pairs, about 2^-48 per operation) */
 #define AW_C64 1            /* complex64 butterflies and phases; FP64 tables and reductions */
-#define AW_C128_FP64 2      /* complex128 state, passes in native FP64 arithmetic */
+#define AW_C128_FP64 2      /* complex128 state, passes in native FP64 arithmetic: the reference's
+                               arithmetic, and what the Python classes use when not told otherwise */
 
 /* device buffers */
 #define AW_BUF_RHO 0        /* rho (WM/WB: Np x Nx in the rotated frame; VN/RB: N x N) */
