@@ -752,6 +752,12 @@ def _group_sets(spec):
     return out
 
 
+def group_member_params(n, k, precision):
+    """Member k (side n) of a group workload: its own harmonic-plus-quartic potential."""
+    return dict(t=0.0, dt=0.01, X_gridDIM=n, X_amplitude=float(np.sqrt(np.pi * n / 2.0)), x0=0.3 * k, p0=-0.2 * k,
+                c2=0.2 + 0.1 * k, K="0.5 * P * P", V="c2 * X * X + 0.01 * X * X * X * X", precision=precision)
+
+
 def run_group(args):
     """Von Neumann propagators of the given sides (default one each of 128, 256, 512, 1024 and 2048; their
     own potentials), 200 steps: grouped (one persistent launch per pass of a step for all of them) against
@@ -768,10 +774,7 @@ def run_group(args):
     for sides in _group_sets(args.sides):
         props = []
         for k, n in enumerate(sides):
-            a = float(np.sqrt(np.pi * n / 2.0))
-            g = RhoVNeumannCUDA1D(t=0.0, dt=0.01, X_gridDIM=n, X_amplitude=a, x0=0.3 * k, p0=-0.2 * k,
-                                  c2=0.2 + 0.1 * k, K="0.5 * P * P", V="c2 * X * X + 0.01 * X * X * X * X",
-                                  precision=args.precision)
+            g = RhoVNeumannCUDA1D(**group_member_params(n, k, args.precision))
             g.set_rho(init)
             props.append(g)
         work = float(sum(n * n for n in sides)) * steps
