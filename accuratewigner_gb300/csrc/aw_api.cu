@@ -897,6 +897,10 @@ static int tune_shapes(aw_state_s* h) {
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   int r = AW_OK;
+  // launches per timing: at least 4, up to 32 on small grids (a 256^2 pass takes about 10 us, and four
+  // of them left the choice to timing noise: the plain 256^2 step measured 0.049 or 0.056 ms by run)
+  const long long pts = (long long)h->nr * h->nc;
+  const int reps = (int)std::max(4LL, std::min(32LL, (4LL << 20) / std::max(pts, 1LL)));
   for (int round = 0; round < 3 && r == AW_OK; ++round)
     for (int pass = 0; pass < 2 && r == AW_OK; ++pass)
       for (int shape = 0; shape < 2 && r == AW_OK; ++shape) {
@@ -918,7 +922,7 @@ static int tune_shapes(aw_state_s* h) {
         float ms = 0.f;
         if (!r) {
           cudaEventRecord(e0, h->st);
-          for (int k = 0; k < 4 && !r; ++k) r = launch_pass(h, a, row ? h->tw_r : h->tw_c, row);
+          for (int k = 0; k < reps && !r; ++k) r = launch_pass(h, a, row ? h->tw_r : h->tw_c, row);
           cudaEventRecord(e1, h->st);
           cudaEventSynchronize(e1);
           cudaEventElapsedTime(&ms, e0, e1);
@@ -929,8 +933,9 @@ static int tune_shapes(aw_state_s* h) {
   cudaEventDestroy(e1);
   if (r) return r;
   TRY(settle(h));
-  const int row_best = (best_of[0][1] >= 0.f && best_of[0][1] < best_of[0][0]) ? 1 : 0;
-  const int col_best = (best_of[1][1] >= 0.f && best_of[1][1] < best_of[1][0]) ? 1 : 0;
+  // the other shape only when it is clearly faster (3 %): near-equal timings keep the size rule's
+  const int row_best = (best_of[0][1] >= 0.f && best_of[0][1] < 0.97f * best_of[0][0]) ? 1 : 0;
+  const int col_best = (best_of[1][1] >= 0.f && best_of[1][1] < 0.97f * best_of[1][0]) ? 1 : 0;
   std::lock_guard<std::mutex> lk(g_tune_mu);
   auto it = g_tuned_shapes.find(key);  // another handle may have tuned first: its choice stands
   if (it == g_tuned_shapes.end()) it = g_tuned_shapes.emplace(key, std::make_pair(row_best, col_best)).first;
