@@ -405,6 +405,7 @@ def run_ours(args):
             "gpu_launches": main["launches"],
             "roofline": main["roofline"],
             "fp64_pipe": fp64_pipe_note(args.precision),
+            "fp64_roofline": fp64_roofline(args.precision, main["value"], main["clocks"]),
             "kernel_profile": main["profile"],
             "forms": forms,
             "clocks": main["clocks"],
@@ -427,6 +428,27 @@ def fp64_pipe_note(precision):
         return json.load(open(path)).get("fp64_pipe")
     except Exception:
         return None
+
+
+def fp64_roofline(precision, value, clocks):
+    """The native FP64 step against the FP64 pipe: the passes' FP64 instructions a point (committed ncu
+    counts) times grid-pt*steps/s, over 2 FP64 lanes a clock a SM at the SM clock sampled during the run."""
+    note = fp64_pipe_note(precision)
+    if not note or "fp64_instructions_per_point" not in note:
+        return None
+    import torch
+
+    per = note["fp64_instructions_per_point"]
+    inst = sum(v for k, v in per.items() if isinstance(v, (int, float)))
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
+    if not mhz:
+        return None
+    peak = 2.0 * torch.cuda.get_device_properties(0).multi_processor_count * mhz * 1e6
+    achieved = inst * value
+    return {"bound": "fp64 pipe", "fp64_inst_per_point_step": inst, "achieved_inst_per_s": achieved,
+            "peak_inst_per_s": peak, "frac": achieved / peak, "sm_mhz": mhz,
+            "note": "FP64 lane instructions of the row, column and marginal passes a grid point a step "
+                    "(profiles/traffic_per_launch.json) x the measured grid-pt*steps/s"}
 
 
 def load_traffic(kernel, precision):
