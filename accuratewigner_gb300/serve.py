@@ -235,9 +235,14 @@ class Pool(threading.Thread):
 class Engine:
     """Continuous-batching request loop on one GPU."""
 
-    def __init__(self, precision="c128", chunk=200, dt=0.01, dbeta=0.01, slots=None, reserve_bytes=2 << 30):
+    def __init__(self, precision="c128", chunk=200, dt=0.01, dbeta=0.01, slots=None, reserve_bytes=2 << 30,
+                 fallback="c128"):
+        """precision: the form of every request, or "auto": complex64 while its measured error allows,
+        else `fallback`, a complex128 form ("c128", double-float, or "c128-fp64", native FP64)."""
         assert precision in ("c128", "c64", "auto", "c128-fp64")
+        assert fallback in ("c128", "c128-fp64")
         self.precision = precision
+        self.fallback = fallback
         self.chunk = chunk
         self.dt = dt
         self.dbeta = dbeta
@@ -260,11 +265,11 @@ class Engine:
         """The form a request starts in (auto: complex64 unless its tolerance is out of its reach)."""
         if self.precision != "auto":
             return self.precision
-        return "c64" if req.tol >= C64_MIN_TOL else "c128"
+        return "c64" if req.tol >= C64_MIN_TOL else self.fallback
 
     def pool(self, kind, n, precision=None):
         """The pool of (kind, n, precision), created when the free device memory covers it."""
-        precision = precision or (self.precision if self.precision != "auto" else "c128")
+        precision = precision or (self.precision if self.precision != "auto" else self.fallback)
         key = (kind, n, precision)
         with self.lock:
             p = self.pools.get(key)
@@ -289,7 +294,7 @@ class Engine:
 
     def warm(self, kinds=("wm", "vn", "rb"), sides=(128, 256, 512, 1024, 2048)):
         """Create the pools ahead of the first request (JIT compile, buffers), as a server starts."""
-        precs = ("c128", "c64") if self.precision == "auto" else (self.precision,)
+        precs = (self.fallback, "c64") if self.precision == "auto" else (self.precision,)
         for k in kinds:
             for n in sides:
                 for p in precs:
@@ -325,7 +330,7 @@ class Engine:
                 got[r.precision] = r
                 if len(got) < 2:
                     return
-            lo, hi = got["c64"], got["c128"]
+            lo, hi = got["c64"], got[self.fallback]
             ref = hi.state
             err = float(np.linalg.norm(lo.state - ref) / max(np.linalg.norm(ref), 1e-300))
             # a Gibbs run that stopped early (purity 1) ends with its probe
@@ -344,7 +349,7 @@ class Engine:
             self._sub(req, left, keep.precision, keep.rho, lambda c: self._complete(req, c, continued=True))
 
         self._sub(req, probe, "c64", None, probe_done)
-        self._sub(req, probe, "c128", None, probe_done)
+        self._sub(req, probe, self.fallback, None, probe_done)
 
     def _complete(self, req, last, continued):
         """Finish an auto request from its last internal request: the probe it kept, or the

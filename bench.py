@@ -637,7 +637,7 @@ def run_served(args):
     steps ~ U(100, 5000), through the continuous-batching request loop."""
     from accuratewigner_gb300.serve import Engine, make_stream
 
-    eng = Engine(precision=args.precision, chunk=200)
+    eng = Engine(precision=args.precision, chunk=200, fallback=args.fallback)
     eng.warm()
     reqs = make_stream(args.requests, args.rate, seed=0)
     for r in reqs:
@@ -655,7 +655,7 @@ def run_served(args):
            "steps": "U(100, 5000)", "kinds": ["wigner-moyal (Ehrenfest)", "von Neumann", "rho-Bloch Gibbs"],
            "potential": "c2 x^2 + c3 x^3 + c4 x^4, c2 ~ U(0.1, 1), c3 ~ U(-0.02, 0.02), c4 ~ U(0, 0.05)",
            "amplitude": "X_amplitude = P_amplitude = sqrt(pi N / 2)", "chunk_steps": 200,
-           "precision": args.precision, "tolerance": args.tol},
+           "precision": args.precision, "tolerance": args.tol, "fallback": args.fallback},
           dict({"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
                 "mean_latency_s": float(lat.mean()), "p50_latency_by_kind_s": by_kind, "clocks": clk.summary()},
                **auto_summary(reqs)))
@@ -680,7 +680,7 @@ def run_served_sweep(args):
     from accuratewigner_gb300.serve import Engine, make_stream
 
     rates = sorted(float(r) for r in args.rates.split(","))
-    eng = Engine(precision=args.precision, chunk=200)
+    eng = Engine(precision=args.precision, chunk=200, fallback=args.fallback)
     eng.warm()
     sweep = []
     with ClockSampler(0) as clk:
@@ -933,6 +933,8 @@ def main():
     ap.add_argument("--requests", type=int, default=60, help="served: number of requests (per rate for the sweep)")
     ap.add_argument("--rate", type=float, default=4.0, help="served: Poisson arrival rate per second")
     ap.add_argument("--rates", default="1,1.5,2,3,4", help="served-sweep: comma-separated arrival rates per second")
+    ap.add_argument("--fallback", default="c128", choices=["c128", "c128-fp64"],
+                    help="served with --precision auto: the complex128 form a request falls back to")
     ap.add_argument("--tol", type=float, default=1e-5,
                     help="served: each request's relative error tolerance (precision auto runs complex64 within it)")
     ap.add_argument("--sides", default="128,256,512,1024,2048",

@@ -52,12 +52,12 @@ class _FakePool:
         (r.on_done or self.engine._finished)(r)
 
 
-def _auto_engine(c64_err):
+def _auto_engine(c64_err, fallback="c128"):
     import numpy as np
 
     from accuratewigner_gb300.serve import Engine
 
-    eng = Engine(precision="auto")
+    eng = Engine(precision="auto", fallback=fallback)
     log = []
     base = np.ones((4, 4), np.complex128)
     eng.pool = lambda kind, n, precision=None: _FakePool(eng, precision, base, c64_err, log)
@@ -106,3 +106,15 @@ def test_auto_routes_unreachable_tolerances_to_complex128():
     assert eng.precision_for(Request(0, "wm", 128, 50, (0.5, 0.0, 0.0), tol=C64_MIN_TOL / 2)) == "c128"
     assert eng.precision_for(Request(0, "wm", 128, 50, (0.5, 0.0, 0.0), tol=1e-5)) == "c64"
     assert Engine(precision="c128").precision_for(Request(0, "wm", 128, 50, (0.5, 0.0, 0.0))) == "c128"
+
+
+def test_auto_falls_back_to_native_fp64_when_asked():
+    """With fallback="c128-fp64" the complex128 probe and the continuation run in native FP64."""
+    from accuratewigner_gb300.serve import PROBE_STEPS, Request
+
+    eng, log = _auto_engine(c64_err=1e-6, fallback="c128-fp64")
+    tight = Request(0, "vn", 256, 900, (0.5, 0.0, 0.0), tol=2e-6)
+    eng.submit(tight)
+    assert [r.precision for r in log] == ["c64", "c128-fp64", "c128-fp64"]
+    assert [r.steps for r in log] == [PROBE_STEPS, PROBE_STEPS, 900 - PROBE_STEPS]
+    assert tight.fell_back and tight.precision == "c128-fp64"
