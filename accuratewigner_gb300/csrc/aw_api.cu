@@ -860,6 +860,23 @@ static int tune_col_lines(aw_state_s* h) {
     for (size_t c = 0; c < cand.size(); ++c)
       if (best_of[c] >= 0.f && (bi == cand.size() || best_of[c] < best_of[bi])) bi = c;
     if (bi == cand.size()) return fail(AW_E_STATE, "no column-pass kernel for a %d x %d grid", h->nr, h->nc);
+    // Native FP64 on a small grid (fewer than two blocks a SM at the fastest width): among the widths
+    // within 3 % of the fastest, the one with the most blocks.  Timed alone, one and two columns a
+    // block are equal at 256 x 256; inside the step, whose marginal pass and observable reduction
+    // overlap the column pass on a second stream, one column a block gave 0.049-0.050 ms a step and
+    // two 0.056-0.057 (the double-float form showed no difference).
+    int dev = 0, sms = 0;
+    if (!h->df && !h->f32 && cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+        (long long)(h->nc / (cand[bi] & 0xff)) * h->ni < 2LL * sms) {
+      size_t wi = bi;
+      for (size_t c = 0; c < cand.size(); ++c) {
+        if (best_of[c] < 0.f || best_of[c] > 1.03f * best_of[bi]) continue;
+        const int lc = cand[c] & 0xff, lw = cand[wi] & 0xff;
+        if (lc < lw || (lc == lw && best_of[c] < best_of[wi])) wi = c;
+      }
+      bi = wi;
+    }
     best = cand[bi];
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1079,6 +1096,15 @@ static int create_impl(const aw_config* cfg, aw_state_s* h, bool check_only = fa
     h->tcoef.push_back(cfg->term_coef[k]);
   }
   if (cfg->n_terms > 64) return fail(AW_E_ARG, "at most 64 observable terms");
+  // every term adds into a slot of its history row, from an expression that exists
+  for (int k = 0; k < cfg->n_terms; ++k) {
+    const int kind = cfg->term_kind[k], idx = cfg->term_index[k];
+    if (cfg->term_slot[k] < 0 || cfg->term_slot[k] >= cfg->n_slots)
+      return fail(AW_E_ARG, "observable term %d: slot %d outside 0..%d", k, cfg->term_slot[k], cfg->n_slots - 1);
+    if ((kind != AW_TERM_X && kind != AW_TERM_P) || idx < 0 ||
+        idx >= (kind == AW_TERM_X ? cfg->n_obs_x : cfg->n_obs_p))
+      return fail(AW_E_ARG, "observable term %d: kind %d, index %d has no expression", k, kind, idx);
+  }
   h->kn.rotated = h->kind == AW_WIGNER_MOYAL || h->kind == AW_WIGNER_BLOCH;
   h->kn.vn = h->kind == AW_RHO_VNEUMANN || h->kind == AW_RHO_BLOCH;
   h->kn.sw = h->kind == AW_SCHRODINGER;

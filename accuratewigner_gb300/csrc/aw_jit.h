@@ -259,6 +259,8 @@ extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw
                                        const double* aw_prm, double* aw_tv, unsigned int* aw_counter, int aw_nchunk) {
   __shared__ double aw_red[256];
   __shared__ double aw_fsum[67];
+  __shared__ double aw_scoef[64];
+  __shared__ int aw_sslot[64], aw_skind[64];
   __shared__ int aw_is_last;
   if (aw_stop && *aw_stop) return;
   const int aw_q = blockIdx.x / aw_nchunk;  // < nterms: a term; nterms: X norm; +1: P norm; +2: squares
@@ -308,6 +310,12 @@ extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw
   __syncthreads();
   if (!aw_is_last) return;
   __threadfence();
+  // the terms' slots, kinds and coefficients, staged for the per-slot sums below
+  for (int aw_k = aw_t; aw_k < aw_nterms; aw_k += aw_nt) {
+    aw_sslot[aw_k] = aw_tslot[aw_k];
+    aw_skind[aw_k] = aw_tkind[aw_k];
+    aw_scoef[aw_k] = aw_tcoef[aw_k];
+  }
   // one warp per term (or norm, or squares): lanes sum over the chunks, then a shuffle tree
   const volatile double* aw_vt = aw_tv;
   const int aw_lane = aw_t & 31;
@@ -318,14 +326,21 @@ extern "C" __global__ void aw_finalize(const double* aw_colsum, const double* aw
     if (aw_lane == 0) aw_fsum[aw_k] = aw_acc;
   }
   __syncthreads();
-  if (aw_t == 0) {
-    const double aw_norm = aw_fsum[aw_nterms] * aw_dXdP;
-    const double aw_pnorm_raw = aw_fsum[aw_nterms + 1];
-    for (int aw_q2 = 0; aw_q2 < aw_nslots; ++aw_q2) aw_hist[aw_q2] = 0.0;
+  const double aw_norm = aw_fsum[aw_nterms] * aw_dXdP;
+  const double aw_pnorm_raw = aw_fsum[aw_nterms + 1];
+  // each slot by its own thread: its terms added in term order from zero, the sums one thread's loop
+  // over the terms into a zeroed row makes, without that loop's chain of dependent global loads and
+  // stores (it was most of this kernel's time on small grids)
+  for (int aw_s2 = aw_t; aw_s2 < aw_nslots; aw_s2 += aw_nt) {
+    double aw_h = 0.0;
     for (int aw_k = 0; aw_k < aw_nterms; ++aw_k) {
-      const bool aw_own = aw_pnorm_own && aw_tkind[aw_k] == 1;
-      aw_hist[aw_tslot[aw_k]] += aw_tcoef[aw_k] * (aw_own ? aw_fsum[aw_k] / aw_pnorm_raw : aw_fsum[aw_k] * aw_dXdP / aw_norm);
+      if (aw_sslot[aw_k] != aw_s2) continue;
+      const bool aw_own = aw_pnorm_own && aw_skind[aw_k] == 1;
+      aw_h += aw_scoef[aw_k] * (aw_own ? aw_fsum[aw_k] / aw_pnorm_raw : aw_fsum[aw_k] * aw_dXdP / aw_norm);
     }
+    aw_hist[aw_s2] = aw_h;
+  }
+  if (aw_t == 0) {
     const double aw_purity = 2.0 * M_PI * aw_fsum[aw_nterms + 2] * aw_dXdP / (aw_norm * aw_norm);
     aw_hist[aw_nslots] = aw_purity;
     aw_hist[aw_nslots + 1] = aw_norm;
@@ -364,6 +379,8 @@ extern "C" __global__ void aw_finalize_rot(const double2* aw_z, const double2* a
   __shared__ double aw_red[256];
   __shared__ double aw_wg[256];
   __shared__ double aw_fsum[66];
+  __shared__ double aw_scoef[64];
+  __shared__ int aw_sslot[64];
   __shared__ int aw_is_last;
   {
     const long long aw_in = blockIdx.y;
@@ -440,6 +457,11 @@ extern "C" __global__ void aw_finalize_rot(const double2* aw_z, const double2* a
   __syncthreads();
   if (aw_is_last) {
     __threadfence();
+    // the terms' slots and coefficients, staged for the per-slot sums below
+    for (int aw_k = aw_t; aw_k < aw_nterms; aw_k += aw_nt) {
+      aw_sslot[aw_k] = aw_tslot[aw_k];
+      aw_scoef[aw_k] = aw_tcoef[aw_k];
+    }
     // one warp per term (or norm, or purity): lane sums over the chunks, then a shuffle tree
     const volatile double* aw_vt = aw_tv;
     const int aw_lane = aw_t & 31;
@@ -450,12 +472,18 @@ extern "C" __global__ void aw_finalize_rot(const double2* aw_z, const double2* a
       if (aw_lane == 0) aw_fsum[aw_k] = aw_acc;
     }
     __syncthreads();
-    if (aw_t == 0) {
-      const double* aw_sum = aw_fsum;
-      const double aw_norm = aw_sum[aw_nterms] * aw_dXdP;
-      for (int aw_k = 0; aw_k < aw_nslots; ++aw_k) aw_hist[aw_k] = 0.0;
+    const double* aw_sum = aw_fsum;
+    const double aw_norm = aw_sum[aw_nterms] * aw_dXdP;
+    // each slot by its own thread: its terms added in term order from zero, the sums one thread's
+    // loop over the terms into a zeroed row makes, without that loop's chain of dependent global
+    // loads and stores (it was most of this kernel's time on small grids)
+    for (int aw_s2 = aw_t; aw_s2 < aw_nslots; aw_s2 += aw_nt) {
+      double aw_h = 0.0;
       for (int aw_k = 0; aw_k < aw_nterms; ++aw_k)
-        aw_hist[aw_tslot[aw_k]] += aw_tcoef[aw_k] * (aw_sum[aw_k] * aw_dXdP / aw_norm);
+        if (aw_sslot[aw_k] == aw_s2) aw_h += aw_scoef[aw_k] * (aw_sum[aw_k] * aw_dXdP / aw_norm);
+      aw_hist[aw_s2] = aw_h;
+    }
+    if (aw_t == 0) {
       const double aw_purity = 2.0 * M_PI * aw_dXdP * aw_nrow * aw_sum[aw_nterms + 1] / (aw_norm * aw_norm);
       aw_hist[aw_nslots] = aw_purity;
       aw_hist[aw_nslots + 1] = aw_norm;

@@ -1,7 +1,8 @@
 /* A C99 caller of include/awigner.h: the header compiles as plain C and the library is usable
  * without Python.  Runs on a machine without a GPU (aw_check_config makes no CUDA runtime call):
  * a harmonic Wigner-Moyal configuration with the Ehrenfest observables is checked, then the same
- * configuration with an expression that does not compile and with a grid that is too small.
+ * configuration with an expression that does not compile, with observable terms outside their
+ * history row or without an expression, and with a grid that is too small.
  * Prints one line per check and exits non-zero on the first unexpected status. */
 #include <stdio.h>
 #include <string.h>
@@ -58,6 +59,14 @@ int main(void) {
   c.V = "0.5 * omega * omega * X * X + no_such_name";
   bad |= expect("undefined name in V", aw_check_config(&c, NULL), AW_E_JIT);
   c.V = "0.5 * omega * omega * X * X";
+  const int32_t slot_out[] = {0, 1, 2, 3, 4, 5};
+  c.term_slot = slot_out;
+  bad |= expect("term slot outside the row", aw_check_config(&c, NULL), AW_E_ARG);
+  c.term_slot = slot;
+  const int32_t index_out[] = {0, 0, 0, 1, 2, 2};
+  c.term_index = index_out;
+  bad |= expect("term without an expression", aw_check_config(&c, NULL), AW_E_ARG);
+  c.term_index = index;
   c.x_grid_dim = 16;
   bad |= expect("16-point grid", aw_check_config(&c, NULL), AW_E_ARG);
   bad |= expect("null configuration", aw_check_config(NULL, NULL), AW_E_ARG);
