@@ -224,9 +224,18 @@ class DeviceArray:
     def ptr(self):
         return self._info()[0]
 
-    def get(self):
+    def get(self, ary=None):
+        """The buffer as a complex128 array: a new one, or `ary` filled in place (a writeable C-contiguous
+        complex128 array of the buffer's shape, e.g. in pinned memory), as pycuda's GPUArray.get(ary)."""
         _, r, c, _ = self._info()
-        out = np.empty((r, c), np.complex128)
+        if ary is None:
+            out = np.empty((r, c), np.complex128)
+        else:
+            out = ary
+            if (not isinstance(out, np.ndarray) or out.dtype != np.complex128 or out.shape != (r, c) or
+                    not out.flags.c_contiguous or not out.flags.writeable):
+                raise ValueError("get(ary): ary must be a writeable C-contiguous complex128 array of shape %s" %
+                                 ((r, c),))
         check(load().aw_get_buffer(self._owner._h, self._which, out.ctypes.data_as(c_vp), 0))
         return out
 

@@ -33,6 +33,25 @@ def test_wigner2rho_rho2wigner_roundtrip():
     assert rel_l2(g.wignerfunction.get(), c.wignerfunction) < TOL
 
 
+def test_get_into_a_given_array():
+    """get(ary) fills a preallocated host array in place (pycuda's GPUArray.get(ary)) with the bits
+    get() returns, and refuses an array of another type or shape."""
+    from accuratewigner_gb300 import WignerMoyalCUDA1D
+
+    g = WignerMoyalCUDA1D(**WM_ANHARMONIC)
+    g.set_wignerfunction(WM_INIT)
+    g.propagate(3)
+    host = np.empty(g.wignerfunction.shape, np.complex128)
+    assert g.wignerfunction.get(host) is host
+    assert np.array_equal(host, g.wignerfunction.get())
+    r, c = host.shape
+    for bad in (np.empty((r, c), np.complex64), np.empty((3, 3), np.complex128),
+                np.empty((r, 2 * c), np.complex128)[:, ::2]):
+        with pytest.raises(ValueError):
+            g.wignerfunction.get(bad)
+    g.close()
+
+
 def test_propagate_ehrenfest_anharmonic():
     from accuratewigner_gb300 import WignerMoyalCUDA1D
     from oracle.propagators import WignerMoyalOracle
