@@ -536,15 +536,21 @@ def _line(workload, metric, value, unit, seconds, args, config, extra=None, high
     print(json.dumps(line))
 
 
-def run_plain(args):
-    """Wigner-Moyal 256 x 256, Xa = 8, Pa = 7, V = x^2 / 2 + 0.05 x^4, dt = 0.01, 1000 steps with Ehrenfest."""
+def plain_propagator(precision):
+    """Wigner-Moyal 256 x 256, Xa = 8, Pa = 7, V = x^2 / 2 + 0.05 x^4, dt = 0.01, Ehrenfest observables."""
     from accuratewigner_gb300 import WignerMoyalCUDA1D
 
     p = dict(t=0.0, dt=0.01, X_gridDIM=256, X_amplitude=8.0, P_gridDIM=256, P_amplitude=7.0, K="0.5 * P * P",
              V="0.5 * X * X + 0.05 * X * X * X * X", diff_K="P", diff_V="X + 0.2 * X * X * X",
-             precision=args.precision)
+             precision=precision)
     g = WignerMoyalCUDA1D(**p)
     g.set_wignerfunction("exp(-pow(X - 1., 2) - P * P) / M_PI")
+    return g
+
+
+def run_plain(args):
+    """The plain 256 x 256 propagator (plain_propagator), 1000 steps in calls of CHUNK."""
+    g = plain_propagator(args.precision)
     for _ in range(2):  # warm-up calls of the timed length (their step-window graphs are captured here)
         g.propagate(CHUNK)
     steps = 1000
@@ -891,12 +897,15 @@ def run_large_vn(args):
 
 
 def run_profile_window(args):
-    """The headline (or the 4096^2 von Neumann) workload with `--profile-steps` steps inside a profiler
-    range: the launches an ncu capture with --profile-from-start off sees are those steps' alone."""
+    """The headline (or the 4096^2 von Neumann, or the plain 256^2) workload with `--profile-steps` steps
+    inside a profiler range: the launches an ncu capture with --profile-from-start off sees are those
+    steps' alone."""
     import torch
 
     torch.cuda.init()
-    if args.workload == "large-vn":
+    if args.workload == "plain":
+        g = plain_propagator(args.precision)
+    elif args.workload == "large-vn":
         from accuratewigner_gb300 import RhoVNeumannCUDA1D
 
         p, rho0 = large_vn_config()
@@ -926,7 +935,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="headline: skip the other arithmetic forms")
     ap.add_argument("--profile-steps", type=int, default=0,
-                    help="set up the workload (headline or large-vn), warm up, run this many steps inside a "
+                    help="set up the workload (headline, plain or large-vn), warm up, run this many steps inside a "
                          "cudaProfilerStart/Stop range (for ncu --profile-from-start off) and exit")
     ap.add_argument("--workload", default="strong-field",
                     choices=["strong-field", "plain", "batched-gibbs", "served", "served-sweep", "large-vn",
