@@ -186,6 +186,7 @@ class RhoVNeumannCUDA1D:
 
     def propagate(self, steps=1):
         lib = _lib.load()
+        steps = max(int(steps), 0)  # the reference loops over xrange(steps): a negative count steps nowhere
         if self.isEhrenfest and not self._native_ehrenfest:
             for _ in range(steps):
                 t = _c.c_double(self.t)

@@ -173,6 +173,7 @@ class SchrodingerWignerCUDA1D:
 
     def propagate(self, steps=1):
         lib = _lib.load()
+        steps = max(int(steps), 0)  # the reference loops over xrange(steps): a negative count steps nowhere
         if self.isEhrenfest and not self._native_ehrenfest:
             raise NotImplementedError("Ehrenfest observables must be functions of X or of P alone")
         t = _c.c_double(self.t)

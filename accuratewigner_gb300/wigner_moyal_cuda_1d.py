@@ -253,6 +253,7 @@ class WignerMoyalCUDA1D:
 
     def propagate(self, steps=1):
         lib = _lib.load()
+        steps = max(int(steps), 0)  # the reference loops over xrange(steps): a negative count steps nowhere
         if (self.isEhrenfest or self.extra_observables) and not self._native_ehrenfest:
             # an observable mixes X and P: step and average one at a time, as the reference does
             for _ in range(steps):
@@ -261,7 +262,7 @@ class WignerMoyalCUDA1D:
                 _lib.check(lib.aw_propagate(self._h, 1, _c.byref(t)))
                 self.t = np.float64(t.value)
                 self._averages_now()
-            if steps == 0:
+            if steps == 0 and not self.isEhrenfest:
                 self.normalize_rho_wigner()
             return self.wignerfunction
         t = _c.c_double(self.t)
