@@ -204,6 +204,9 @@ struct aw_state_s {
   // native FP64 on grids up to 1024 x 1024: the shear factors of the per-step Wigner transform as full
   // [lines][positions] tables (one complex product a point fewer on the FP64 pipe)
   DevBuf shx_full, shy_full;
+  // ... and the column pass's K kick with its 1/N^2 (real time, K independent of t, one instance, no
+  // momentum absorber) as one [column][row] table, rebuilt by each propagation call
+  DevBuf kfull;
   DevBuf tabs;                         // phase tables, slots of (nc + nr) complex
   DevBuf vseq, vtimes;                 // time-dependent kick tables of a run of time points, their times
   DevBuf maskx, maskp;                 // 2-D masks (rotated frame)
@@ -1386,7 +1389,7 @@ extern "C" int aw_destroy(aw_handle h) {
                     &h->terms, &h->part, &h->blk_tabs, &h->params, &h->bvec, &h->maskx2, &h->masksep,
                     &h->hwin, &h->ctimes, &h->tt_r[0], &h->tt_r[1], &h->tt_c[0], &h->tt_c[1], &h->tt_w[0],
                     &h->tt_w[1], &h->tt_l1[0], &h->tt_l1[1], &h->tt_l2[0], &h->tt_l2[1], &h->shx_full,
-                    &h->shy_full};
+                    &h->shy_full, &h->kfull};
   for (DevBuf* b : bufs) dfree(*b);
   for (DevBuf& b : h->sw_states) dfree(b);
   for (auto& g : h->graph_exec)
@@ -2101,6 +2104,15 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
 
   if (!vdep) TRY(rot_tables_V(h, p, times[1], times[1], false));
   if (!kdep) TRY(rot_tables_K(h, p, times[1]));
+  // Native FP64 real time with a K kick that does not change during the call: the kick and the 1/N^2 the
+  // column pass folds into it (when no per-call scale is read) as one full table where the full shear
+  // tables exist, so that the FP64-bound column pass makes one complex product a point instead of two
+  // (the line constant and the table along the line)
+  const bool kfull = h->shy_full.p && !p.bloch && !kdep && h->ni == 1 && !c.absp_mode && !(p.ehrenfest && !defer);
+  if (kfull) {
+    if (!h->kfull.p) TRY(dalloc(h->kfull, (size_t)grid * 16));
+    KL(aw_k_sep_full(tab_col(h, TAB_K), tab_row(h, TAB_K), inv_n2, h->nr, h->nc, h->kfull.p, h->st));
+  }
   // With a time-dependent V the kick tables of up to VSEQ consecutive time points are built by one
   // launch: table s of the run holds exp(-i dt/2 V(., t_{n0+s} + dt/2)).
   const long long VSEQ = 256;
@@ -2184,6 +2196,11 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
         }
         a.f1.mask = h->maskp.p;
         a.f1.mask_pow = 1;
+      }
+      if (kfull) {
+        a.f1 = fnone();
+        a.f1.sh_full = h->kfull.p;
+        a.f1.active = 1;
       }
       a.d2 = +1;
       a.stop = stop;

@@ -259,6 +259,19 @@ __global__ void k_shear_full(const double2* hi, const double2* lo, int lo_n, int
   }
 }
 
+// A separable column-pass factor as one table, per column line j and position (row) i:
+//   full[j][i] = conj(row[i]) * (scale * col[j])
+// the product a column tile otherwise forms from the line's constant and the table along the line
+// (complex128)
+__global__ void k_sep_full(const double2* col, const double2* row, double scale, int nr, int nc, double2* full) {
+  const long long n = (long long)nr * nc;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(k / nr), i = (int)(k % nr);
+    const double2 c = make_double2(scale * col[j].x, scale * col[j].y), r = row[i];
+    full[k] = make_double2(r.x * c.x + r.y * c.y, r.x * c.y - r.y * c.x);
+  }
+}
+
 // The von Neumann momentum diagonal from the diagonal sums G of the branch point (aw_api.cu, vn_run):
 // Re M_k = scale Re Sum_d G_d exp(-2 pi i k d / N), N = n1 n2, in two launches of direct FP64 DFTs
 // (the four-step factorisation, d = d1 + n1 d2, k = k2 + n2 k1):
@@ -357,6 +370,12 @@ extern "C" {
 int aw_k_shear_full(const void* hi, const void* lo, int lo_n, int lines, int npos, void* full, void* s) {
   k_shear_full<<<grid_for((long long)lines * npos), 256, 0, (cudaStream_t)s>>>(
       (const double2*)hi, (const double2*)lo, lo_n, lines, npos, (double2*)full);
+  return ok();
+}
+
+int aw_k_sep_full(const void* col, const void* row, double scale, int nr, int nc, void* full, void* s) {
+  k_sep_full<<<grid_for((long long)nr * nc), 256, 0, (cudaStream_t)s>>>((const double2*)col, (const double2*)row, scale,
+                                                                          nr, nc, (double2*)full);
   return ok();
 }
 

@@ -9,6 +9,8 @@ extern "C" {
 int aw_k_scale(void* a, int f32, long long n, double re, double im, const double* ptr, void* s);
 // complex128 shear factors of `lines` lines of npos positions from their hi x lo tables
 int aw_k_shear_full(const void* hi, const void* lo, int lo_n, int lines, int npos, void* full, void* s);
+// full[j * nr + i] = conj(row[i]) * (scale * col[j]) (complex128): a column-pass factor as one table
+int aw_k_sep_full(const void* col, const void* row, double scale, int nr, int nc, void* full, void* s);
 // ninst instances of n elements, instance k scaled by ptr[2k..2k+1] (when ptr)
 int aw_k_scale_n(void* a, int f32, long long n, int ninst, double re, double im, const double* ptr, void* s);
 /* count tables of n complex entries, stride entries apart, each entry k times the real s[k] */
