@@ -2665,11 +2665,10 @@ static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::ve
     const bool last = n == steps;
     {
       if (kdep) TRY(build_tab(h, TAB_K, 1, 0, times[n] + 0.5 * c.dt, 0.0, -c.dt, 0.0, 0.0, c.absp_mode ? 1 : 0, 0.0));
+      // the previous step's 1/trace is applied by the row pass below, with its V kick's line constant
+      // (every pass between is linear): one product a line there instead of one a point here
       AwPassArgs a = pnone(h);
       a.in = a.out = h->rho.p;
-      a.f0 = fnone();
-      a.f0.scale_ptr = dinv(h);
-      a.f0.active = 1;
       a.d1 = -1;
       a.f1 = ftab(h, kslot);
       a.d2 = +1;
@@ -2691,6 +2690,7 @@ static int vn_run(aw_state_s* h, const VnPlan& p, long long steps, const std::ve
       a.d1 = -1;
       a.shape = h->tuned_row_shape;
       a.f1 = ftab(h, vslot);
+      a.f1.scale_ptr = dinv(h);  // 1/trace of the previous step (see the column pass)
       a.diag_out = (double2*)h->diag.p;
       if (p.stop_on_purity || p.bloch) a.red_abs2 = (double*)h->abs2.p;
       if (p.keep_rho) {
@@ -2898,7 +2898,7 @@ static int group_run(aw_handle* hs, int count, int64_t steps, double** tp) {
   }
   for (long long n = 1; n <= steps; ++n) {
     const bool last = n == steps;
-    for (int m = 0; m < count; ++m) {  // column pass: 1/trace, ifft0, K kick, fft0
+    for (int m = 0; m < count; ++m) {  // column pass: 1/trace, ifft0, K kick, fft0 (grouped members)
       aw_state_s* h = hs[m];
       AwPassArgs a = pnone(h);
       a.in = a.out = h->rho.p;
