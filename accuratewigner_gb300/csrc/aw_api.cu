@@ -2177,18 +2177,13 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
       if (kdep) TRY(rot_tables_K(h, p, times[n]));
       AwPassArgs a = pnone(h);
       a.in = a.out = h->rho.p;
-      a.f0 = fnone();
-      a.f0.scale = inv_n2;
-      a.f0.scale_ptr = p.ehrenfest && !defer ? dinv(h) : nullptr;
-      a.f0.active = 1;
       a.d1 = -1;
       a.f1 = ftab(h, p.bloch ? TAB_BK : TAB_K);
-      if (!a.f0.scale_ptr) {
-        // 1/N^2 is a power of two: applied after ifft0, folded into the K kick's per-column constant,
-        // it gives the same bits and saves a complex product a point
-        a.f0 = fnone();
-        a.f1.scale = inv_n2;
-      }
+      // the scale (1/N^2, and with per-step observables and no side stream the previous step's 1/norm)
+      // applied after ifft0 (linear), folded into the K kick's per-column constant: a complex product a
+      // point fewer than scaling before the transform (1/N^2 alone, a power of two, gives the same bits)
+      a.f1.scale = inv_n2;
+      a.f1.scale_ptr = p.ehrenfest && !defer ? dinv(h) : nullptr;
       if (!p.bloch && c.absp_mode) {
         if (c.absp_mode == 2 || !h->maskp_ready) {
           TRY(build_mask2d(h, 1, times[n]));
