@@ -207,6 +207,7 @@ struct aw_state_s {
   // ... and the column pass's K kick with its 1/N^2 (real time, K independent of t, one instance, no
   // momentum absorber) as one [column][row] table, rebuilt by each propagation call
   DevBuf kfull;
+  DevBuf vfull;                        // ... and a V kick that does not change during the call, [row][column]
   DevBuf tabs;                         // phase tables, slots of (nc + nr) complex
   DevBuf vseq, vtimes;                 // time-dependent kick tables of a run of time points, their times
   DevBuf maskx, maskp;                 // 2-D masks (rotated frame)
@@ -1389,7 +1390,7 @@ extern "C" int aw_destroy(aw_handle h) {
                     &h->terms, &h->part, &h->blk_tabs, &h->params, &h->bvec, &h->maskx2, &h->masksep,
                     &h->hwin, &h->ctimes, &h->tt_r[0], &h->tt_r[1], &h->tt_c[0], &h->tt_c[1], &h->tt_w[0],
                     &h->tt_w[1], &h->tt_l1[0], &h->tt_l1[1], &h->tt_l2[0], &h->tt_l2[1], &h->shx_full,
-                    &h->shy_full, &h->kfull};
+                    &h->shy_full, &h->kfull, &h->vfull};
   for (DevBuf* b : bufs) dfree(*b);
   for (DevBuf& b : h->sw_states) dfree(b);
   for (auto& g : h->graph_exec)
@@ -2111,7 +2112,14 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
   const bool kfull = h->shy_full.p && !p.bloch && !kdep && h->ni == 1 && !c.absp_mode && !(p.ehrenfest && !defer);
   if (kfull) {
     if (!h->kfull.p) TRY(dalloc(h->kfull, (size_t)grid * 16));
-    KL(aw_k_sep_full(tab_col(h, TAB_K), tab_row(h, TAB_K), inv_n2, h->nr, h->nc, h->kfull.p, h->st));
+    KL(aw_k_sep_full(tab_col(h, TAB_K), tab_row(h, TAB_K), inv_n2, h->nr, h->nc, 0, h->kfull.p, h->st));
+  }
+  // the same for a V kick that does not change during the call (no 2-D x mask left after folding):
+  // the row pass applies it twice a step, each one complex product a point instead of two
+  const bool vfull = h->shx_full.p && !p.bloch && !vdep && h->ni == 1 && !(c.absx_mode && !h->maskx_sep);
+  if (vfull) {
+    if (!h->vfull.p) TRY(dalloc(h->vfull, (size_t)grid * 16));
+    KL(aw_k_sep_full(tab_col(h, TAB_V1), tab_row(h, TAB_V1), 1.0, h->nr, h->nc, 1, h->vfull.p, h->st));
   }
   // With a time-dependent V the kick tables of up to VSEQ consecutive time points are built by one
   // launch: table s of the run holds exp(-i dt/2 V(., t_{n0+s} + dt/2)).
@@ -2124,6 +2132,13 @@ static int rot_run(aw_state_s* h, const StepPlan& p, long long steps, const std:
   // kick factor of time point n (table slot TAB_V1 when V does not depend on time)
   auto vfactor = [&](long long n, bool sign, AwFactor* f) -> int {
     TRY(vkick(h, p, TAB_V1, sign, times[n], f, n));
+    if (vfull) {
+      *f = fnone();
+      f->sign = sign;
+      f->sh_full = h->vfull.p;
+      f->active = 1;
+      return AW_OK;
+    }
     if (!vdep) return AW_OK;
     const long long need_hi = std::min(n + 1, steps + 1);
     if (n < vs_n0 || need_hi >= vs_n0 + vs_cnt) {

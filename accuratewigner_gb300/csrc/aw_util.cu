@@ -259,14 +259,15 @@ __global__ void k_shear_full(const double2* hi, const double2* lo, int lo_n, int
   }
 }
 
-// A separable column-pass factor as one table, per column line j and position (row) i:
-//   full[j][i] = conj(row[i]) * (scale * col[j])
-// the product a column tile otherwise forms from the line's constant and the table along the line
-// (complex128)
-__global__ void k_sep_full(const double2* col, const double2* row, double scale, int nr, int nc, double2* full) {
+// A separable factor as one table of conj(row[i]) * (scale * col[j]) (complex128), the product a tile
+// otherwise forms from its line's constant and the table along the line: per column line j and
+// position (row) i, full[j][i], for a column pass; per row line i and position j, full[i][j], for a
+// row pass (row_lines)
+__global__ void k_sep_full(const double2* col, const double2* row, double scale, int nr, int nc, int row_lines,
+                           double2* full) {
   const long long n = (long long)nr * nc;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
-    const int j = (int)(k / nr), i = (int)(k % nr);
+    const int j = row_lines ? (int)(k % nc) : (int)(k / nr), i = row_lines ? (int)(k / nc) : (int)(k % nr);
     const double2 c = make_double2(scale * col[j].x, scale * col[j].y), r = row[i];
     full[k] = make_double2(r.x * c.x + r.y * c.y, r.x * c.y - r.y * c.x);
   }
@@ -373,9 +374,9 @@ int aw_k_shear_full(const void* hi, const void* lo, int lo_n, int lines, int npo
   return ok();
 }
 
-int aw_k_sep_full(const void* col, const void* row, double scale, int nr, int nc, void* full, void* s) {
+int aw_k_sep_full(const void* col, const void* row, double scale, int nr, int nc, int row_lines, void* full, void* s) {
   k_sep_full<<<grid_for((long long)nr * nc), 256, 0, (cudaStream_t)s>>>((const double2*)col, (const double2*)row, scale,
-                                                                          nr, nc, (double2*)full);
+                                                                          nr, nc, row_lines, (double2*)full);
   return ok();
 }
 

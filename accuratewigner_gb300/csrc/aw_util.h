@@ -9,8 +9,9 @@ extern "C" {
 int aw_k_scale(void* a, int f32, long long n, double re, double im, const double* ptr, void* s);
 // complex128 shear factors of `lines` lines of npos positions from their hi x lo tables
 int aw_k_shear_full(const void* hi, const void* lo, int lo_n, int lines, int npos, void* full, void* s);
-// full[j * nr + i] = conj(row[i]) * (scale * col[j]) (complex128): a column-pass factor as one table
-int aw_k_sep_full(const void* col, const void* row, double scale, int nr, int nc, void* full, void* s);
+// conj(row[i]) * (scale * col[j]) (complex128) at full[j * nr + i] (a column-pass factor as one table) or,
+// with row_lines, at full[i * nc + j] (a row-pass factor)
+int aw_k_sep_full(const void* col, const void* row, double scale, int nr, int nc, int row_lines, void* full, void* s);
 // ninst instances of n elements, instance k scaled by ptr[2k..2k+1] (when ptr)
 int aw_k_scale_n(void* a, int f32, long long n, int ninst, double re, double im, const double* ptr, void* s);
 /* count tables of n complex entries, stride entries apart, each entry k times the real s[k] */
