@@ -431,20 +431,23 @@ def fp64_pipe_note(precision):
         return None
 
 
-def fp64_roofline(precision, value, clocks):
+def fp64_roofline(precision, value, clocks, sms=None):
     """The native FP64 step against the FP64 pipe: the passes' FP64 instructions a point (committed ncu
-    counts) times grid-pt*steps/s, over 2 FP64 lanes a clock a SM at the SM clock sampled during the run."""
+    counts; the per-call launches left out) times grid-pt*steps/s, over 2 FP64 lanes a clock a SM at the
+    SM clock sampled during the run (sms: the SM count, by default the device's)."""
     note = fp64_pipe_note(precision)
     if not note or "fp64_instructions_per_point" not in note:
         return None
-    import torch
-
     per = note["fp64_instructions_per_point"]
     inst = sum(v for k, v in per.items() if isinstance(v, (int, float)))
     mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
     if not mhz:
         return None
-    peak = 2.0 * torch.cuda.get_device_properties(0).multi_processor_count * mhz * 1e6
+    if sms is None:
+        import torch
+
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+    peak = 2.0 * sms * mhz * 1e6
     achieved = inst * value
     return {"bound": "fp64 pipe", "fp64_inst_per_point_step": inst, "achieved_inst_per_s": achieved,
             "peak_inst_per_s": peak, "frac": achieved / peak, "sm_mhz": mhz,
