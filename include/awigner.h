@@ -198,7 +198,13 @@ int aw_profile_read(aw_handle h, double* ms, double* bytes, int64_t* launches);
  * schrodinger_wigner_cuda_1d.py:26-303): NVRTC compiles the expression
  * strings (SourceModule in the reference), device buffers are allocated and
  * the FFT twiddles and shear tables are built.  Bloch kinds also evaluate
- * V_min and K_min (wigner_bloch_cuda_1d.py:70-92, rho_bloch_cuda_1d.py:70-98). */
+ * V_min and K_min (wigner_bloch_cuda_1d.py:70-92, rho_bloch_cuda_1d.py:70-98).
+ * Device memory: a few grid-sized complex buffers (state, Wigner function,
+ * scratch); a single native FP64 Wigner-Moyal / Wigner-Bloch propagator of
+ * up to 1024 x 1024 points also keeps full shear tables and, once it
+ * propagates in real time, full K-kick and (for a V that does not depend on
+ * t) V-kick tables: up to four more grid-sized complex128 arrays (16 MB each
+ * at 1024 x 1024), which save FP64 products in its passes. */
 int aw_create(const aw_config* cfg, aw_handle* out);
 int aw_destroy(aw_handle h);
 /* The checks of aw_create without a device: the configuration is validated and the expression
